@@ -1,0 +1,231 @@
+/*
+ * acogpu.h -- C ABI of the GB300 Ant Colony Optimization engine for the
+ * symmetric Euclidean TSP.
+ *
+ * This is the drop-in boundary for the reference's `Colony` / `AntSystem` /
+ * `RankBasedAntSystem` C++ surface (reference: inc/Colony.h:24-155,
+ * inc/AntSystem.h:7-23, inc/RankBasedAntSystem.h:12-28).  Every entry point
+ * takes plain pointers and sizes, returns an int status (ACO_OK == 0) and
+ * never throws or exits; aco_colony_last_error() gives the message.  The
+ * reference instead prints and calls exit(EXIT_FAILURE) on any CUDA error
+ * (inc/helper_cuda.h:316-325); the C++ classes in acogpu_colony.hpp keep that
+ * behaviour on top of this ABI.
+ *
+ * One colony lives on one GPU (the current device when it is created) and
+ * runs its kernels on one CUDA stream.  Calls on one colony are not
+ * thread-safe; different colonies are independent.
+ *
+ * Thread safety, ownership: the library copies the distance matrix (or
+ * builds it from coordinates) into its own device layout; the caller keeps
+ * ownership of every pointer it passes.
+ */
+#ifndef ACOGPU_H
+#define ACOGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ACOGPU_VERSION_MAJOR 1
+#define ACOGPU_VERSION_MINOR 0
+
+/* MAX_DISTANCE of the reference (inc/def.h:69): the diagonal of the
+ * distance matrix. */
+#define ACO_MAX_DISTANCE 0x7fffffff
+
+/* ---- status codes ------------------------------------------------------ */
+enum aco_status {
+  ACO_OK = 0,
+  ACO_ERR_INVALID_ARGUMENT = 1,
+  ACO_ERR_OUT_OF_MEMORY = 2,
+  ACO_ERR_CUDA = 3,
+  ACO_ERR_NOT_INITIALIZED = 4,
+  ACO_ERR_UNSUPPORTED = 5,
+  ACO_ERR_DEVICE_TIMEOUT = 6, /* a bounded device-side wait gave up */
+  ACO_ERR_DEVICE_CHECK = 7    /* a device-side consistency check failed */
+};
+
+/* ---- parameter enums ----------------------------------------------------- */
+enum aco_variant {
+  ACO_ANT_SYSTEM = 0,  /* AntSystem: all ants deposit 1/L (src/AntSystem.cu:235-318) */
+  ACO_RANK_BASED = 1   /* RankBasedAntSystem: w-1 ranked ants + best-so-far
+                          (Bullnheimer, Hartl & Strauss 1999); the reference's
+                          update is an empty stub (src/RankBasedAntSystem.cu:48-56) */
+};
+
+enum aco_nn_order {
+  ACO_NN_STABLE = 0,          /* rows sorted by (distance, city): the order of the
+                                 reference GPU kernel (inc/Colony.cuh:101-123) */
+  ACO_NN_REFERENCE_QSORT = 1  /* the permutation of the reference CPU quicksort
+                                 Utils::sort2 (src/Utils.cu:136-159), ties included */
+};
+
+enum aco_heuristic_mode {
+  ACO_HEURISTIC_DEVICE = 0, /* eta = (1/d)^beta on the GPU, correctly rounded for
+                               integer beta in [0, 64] */
+  ACO_HEURISTIC_LIBM = 1    /* eta = powf((float)(1.0/(double)(float)d), beta)
+                               through the host C library, as the reference CPU path
+                               (inc/Colony.h:20); evaluated once per distinct
+                               distance into a table that the GPU expands */
+};
+
+enum aco_fallback {
+  ACO_FALLBACK_REFERENCE = 0, /* select_local_best: the LAST unvisited city of the
+                                 full nn row (inc/Colony.cuh:33-43); needs a full row */
+  ACO_FALLBACK_BEST = 1       /* the unvisited city with the largest choice value,
+                                 lowest index on ties (choose_best_next of ACOTSP) */
+};
+
+enum aco_deposit_mode {
+  ACO_DEPOSIT_DETERMINISTIC = 0, /* row-owned ordered fold: bit-exact with the
+                                    reference's sequential CPU update */
+  ACO_DEPOSIT_ATOMIC = 1         /* red.global.add.f32; order-free, fastest */
+};
+
+enum aco_tau0_mode {
+  ACO_TAU0_REFERENCE = 0, /* 1e-6 (src/AntSystem.cu:200-203, inc/default.h:15) */
+  ACO_TAU0_DORIGO = 1,    /* AS: m / C_nn, RBAS: 0.5 w (w-1) / (rho C_nn), with
+                             C_nn the greedy nearest-neighbour tour from city 0 */
+  ACO_TAU0_VALUE = 2      /* aco_params.tau0 */
+};
+
+/* Stage timers filled by aco_colony_construct_solution, indexed like the
+ * reference's StatsTimer enum (inc/Statistics.h:7-15). */
+enum aco_timer {
+  ACO_TIME_INIT_TOUR = 0,
+  ACO_TIME_TOUR = 1,
+  ACO_TIME_COMPUTE_ANT_DISTANCE = 2,
+  ACO_TIME_EVAPORATE_PHEROMONE = 3,
+  ACO_TIME_UPDATE_PHEROMONE = 4,
+  ACO_TIME_COMPUTE_PROBABILITIES = 5,
+  ACO_TOTAL_TIMERS = 6
+};
+
+typedef struct aco_params {
+  int32_t variant;   /* enum aco_variant */
+  int32_t num_ants;  /* m */
+  float alpha;       /* stored; the reference ignores it (inc/Colony.cuh:29-30)
+                        unless use_alpha is set */
+  float beta;
+  float rho;
+  int32_t use_alpha; /* 0: choice = tau * eta^beta exactly as the reference */
+  int32_t cand_k;    /* candidate-list length; <= 0 or >= n means the full row */
+  int32_t nn_order;  /* enum aco_nn_order */
+  int32_t heuristic; /* enum aco_heuristic_mode */
+  int32_t fallback;  /* enum aco_fallback */
+  int32_t deposit;   /* enum aco_deposit_mode */
+  int32_t tau0_mode; /* enum aco_tau0_mode */
+  float tau0;        /* used when tau0_mode == ACO_TAU0_VALUE */
+  int32_t rank_w;    /* RBAS w (reference default 5, inc/default.h:19) */
+  int32_t aging;     /* 0: noaging variant, 1: aging variant */
+  /* aging parameters (reference: inc/Colony.h:118-124, defaults inc/default.h:34-39) */
+  int32_t min_retirement_age;
+  int32_t max_retirement_age;
+  int32_t local_performance;
+  int32_t global_performance;
+  int32_t min_population_limit;
+  int32_t max_population_limit;
+  int32_t broker;    /* accepted for the broker/nobroker variant; the reference's
+                        broker build defines a flag and nothing else
+                        (inc/broker/parallel.h:3, inc/Colony.h:142-149) */
+  uint64_t seed;     /* seed of the injected uniform stream (acogpu_rng.h) */
+  int32_t ants_per_block; /* construction warps per CTA; 0 = tuned default */
+  int32_t reserved[7];
+} aco_params;
+
+/* Reference defaults (inc/default.h, src/Colony.cu:31-36): AS, m = 10,
+ * alpha 1, beta 5, rho 0.1, full-row candidates, reference quicksort order,
+ * libm heuristic, reference fallback, deterministic deposit, tau0 = 1e-6,
+ * w = 5, noaging, aging parameters 30/50/10/10/40/100, seed 12345678. */
+void aco_params_default(aco_params *p);
+
+typedef struct aco_colony aco_colony;
+
+/* Create a colony on the current device.
+ *   dist: n*n int32 row-major EUC_2D distances with ACO_MAX_DISTANCE on the
+ *         diagonal (the reference's distance vector, src/Setup.cpp:54-70).
+ *   dist_on_device: 0 if dist is host memory, 1 if it is device memory on the
+ *         current device (the reference GPU build passes a device pointer,
+ *         src/Setup.cpp:60-66).
+ * Replaces the constructors AntSystem::AntSystem (src/AntSystem.cu:160-182),
+ * RankBasedAntSystem::RankBasedAntSystem (src/RankBasedAntSystem.cu:14-18)
+ * and Colony::Colony (src/Colony.cu:25-137). */
+int aco_colony_create(const aco_params *params, const int32_t *dist, int32_t n,
+                      int32_t dist_on_device, aco_colony **out);
+
+/* Create a colony from float coordinates; the EUC_2D distance matrix
+ * (reference: Utils::compute_distance, src/Utils.cu:162-182,212-218) is built
+ * on the GPU. */
+int aco_colony_create_coords(const aco_params *params, const float *x,
+                             const float *y, int32_t n, aco_colony **out);
+
+/* Colony::initialize (src/Colony.cu:185-214): initial pheromone, heuristic,
+ * nn-list, aging state, best-so-far reset. */
+int aco_colony_initialize(aco_colony *c);
+
+/* Colony::constructSolution (src/Colony.cu:537-594): one iteration.  timers
+ * (may be NULL) receives per-stage device times in ms, indexed by
+ * enum aco_timer; passing timers makes the call synchronous. */
+int aco_colony_construct_solution(aco_colony *c, float *timers_ms);
+
+/* Run `iterations` iterations back to back from a captured CUDA graph, with
+ * no host synchronisation in between.  Returns once they are enqueued. */
+int aco_colony_run(aco_colony *c, int32_t iterations);
+
+/* Wait for all enqueued work; reports device-side errors. */
+int aco_colony_synchronize(aco_colony *c);
+
+/* Getters of the reference surface (inc/Colony.h:38-48,152). */
+int aco_colony_get_iter_best(aco_colony *c, int64_t *out);  /* getIterBestDist */
+int aco_colony_get_glob_best(aco_colony *c, int64_t *out);  /* getGlobBestDist */
+int aco_colony_get_num_valid_ants(aco_colony *c, int32_t *out); /* getNumValidAnts */
+int aco_colony_get_best_tour(aco_colony *c, int32_t *out_n);   /* getTour, 0-based */
+int aco_colony_get_iteration(aco_colony *c, int32_t *out);
+int aco_colony_get_reps(aco_colony *c, int32_t *out);        /* getReps (always 0) */
+int aco_colony_get_size(aco_colony *c, int32_t *n, int32_t *m, int32_t *k);
+int aco_colony_get_params(aco_colony *c, aco_params *out);
+/* Setters of the reference surface: setAlpha/setBeta/setRho/setOptimum
+ * (inc/Colony.h:35-37,49), RankBasedAntSystem::setW, and the aging setters
+ * (inc/Colony.h:128-139).  beta, w and tau0-relevant values take effect at
+ * the next aco_colony_initialize. */
+int aco_colony_set_alpha(aco_colony *c, float v);
+int aco_colony_set_beta(aco_colony *c, float v);
+int aco_colony_set_rho(aco_colony *c, float v);
+int aco_colony_set_optimum(aco_colony *c, int64_t v);
+int aco_colony_set_rank_w(aco_colony *c, int32_t w);
+int aco_colony_set_aging_params(aco_colony *c, const int32_t six[6]);
+/* antSystemName(): "Ant System" or "Rank-based Ant System". */
+const char *aco_colony_name(const aco_colony *c);
+
+/* State export/import (host buffers), for checking and checkpointing. */
+int aco_colony_read_pheromone(aco_colony *c, float *out_nn);      /* n*n */
+int aco_colony_write_pheromone(aco_colony *c, const float *in_nn);
+int aco_colony_read_heuristic(aco_colony *c, float *out_nn);      /* n*n */
+int aco_colony_read_choice_info(aco_colony *c, float *out_nn);    /* n*n */
+int aco_colony_read_nn_list(aco_colony *c, int32_t *out_nk);      /* n*k */
+int aco_colony_read_distances(aco_colony *c, int32_t *out_nn);    /* n*n */
+int aco_colony_read_tours(aco_colony *c, int32_t *out_mn);        /* m*n */
+int aco_colony_read_tour_lengths(aco_colony *c, int64_t *out_m);
+/* age[m], performance[m], valid[m], pheromone row means[n],
+ * misc[2] = {isconverged, globalperformance} */
+int aco_colony_read_aging(aco_colony *c, int32_t *age, int32_t *perf,
+                          uint8_t *valid, float *mean, int32_t *misc);
+
+/* Bind the colony to a CUDA stream (cudaStream_t passed as void*). */
+int aco_colony_set_stream(aco_colony *c, void *stream);
+/* Number of kernel launches this colony has issued (graph nodes count once
+ * per replay). */
+int aco_colony_get_launch_count(aco_colony *c, int64_t *out);
+
+const char *aco_colony_last_error(const aco_colony *c);
+const char *aco_status_string(int status);
+void aco_colony_destroy(aco_colony *c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ACOGPU_H */
