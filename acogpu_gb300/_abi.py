@@ -23,6 +23,7 @@ ACO_HEURISTIC_DEVICE, ACO_HEURISTIC_LIBM = 0, 1
 ACO_FALLBACK_REFERENCE, ACO_FALLBACK_BEST = 0, 1
 ACO_DEPOSIT_DETERMINISTIC, ACO_DEPOSIT_ATOMIC = 0, 1
 ACO_TAU0_REFERENCE, ACO_TAU0_DORIGO, ACO_TAU0_VALUE = 0, 1, 2
+ACO_CONSTRUCT_AUTO, ACO_CONSTRUCT_GLOBAL, ACO_CONSTRUCT_STAGED = 0, 1, 2
 
 TIMER_NAMES = ("init_tour", "tour", "compute_ant_distance", "evaporate_pheromone",
                "update_pheromone", "compute_probabilities")
@@ -54,7 +55,22 @@ class AcoParams(ctypes.Structure):
         ("broker", ctypes.c_int32),
         ("seed", ctypes.c_uint64),
         ("ants_per_block", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("construct_mode", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
+    ]
+
+
+class AcoStats(ctypes.Structure):
+    _fields_ = [
+        ("iteration", ctypes.c_int64),
+        ("tours_built", ctypes.c_int64),
+        ("fallbacks", ctypes.c_int64),
+        ("greedy_length", ctypes.c_int64),
+        ("iter_best", ctypes.c_int64),
+        ("glob_best", ctypes.c_int64),
+        ("num_valid", ctypes.c_int32),
+        ("tau0", ctypes.c_float),
+        ("reserved", ctypes.c_int64 * 4),
     ]
 
 

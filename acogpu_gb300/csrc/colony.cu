@@ -1,0 +1,745 @@
+// colony.cu -- host implementation of the C ABI in include/acogpu.h.
+//
+// One colony = one set of device buffers (layout in aco_device.cuh) + one
+// stream.  An iteration is three kernels (construct, epilogue, pheromone
+// rows), or five in atomic-deposit mode, with no host synchronisation; the
+// iteration is captured once into a CUDA graph and replayed by
+// aco_colony_run.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+#include <string>
+#include <vector>
+
+#include "acogpu.h"
+#include "aco_kernels.h"
+
+using namespace aco;
+
+struct aco_colony {
+  aco_params p;
+  int n = 0, m = 0, K = 0, ld = 0, ldk = 0, ldm = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int32_t *dist = nullptr;
+  float *eta = nullptr, *tau = nullptr, *choice = nullptr;
+  int32_t *nn = nullptr;
+  float *eta_nn = nullptr, *tau_nn = nullptr, *choice_nn = nullptr;
+  int32_t *tours = nullptr;
+  int64_t *newlen = nullptr, *len = nullptr;
+  int32_t *succT = nullptr, *predT = nullptr, *gbtour = nullptr;
+  int32_t *age = nullptr, *perf = nullptr;
+  uint8_t *valid = nullptr;
+  float *mean = nullptr;
+  int32_t *dep_col = nullptr;
+  float *dep_delta = nullptr;
+  ColonyState *st = nullptr;
+  int16_t *nn16 = nullptr;  // candidate ids as int16, 32 per row (staged kernel)
+  bool staged = false;
+  int staged_grid = 0, staged_warps = 0;
+  int num_sms = 0, max_smem_optin = 0;
+  std::vector<void *> allocations;
+  bool initialized = false;
+  int64_t optimum = -1;
+  int apb = 4;
+  int64_t launches = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::string err;
+};
+
+namespace {
+
+const char *kNameAS = "Ant System";             // src/AntSystem.cu:7
+const char *kNameRBAS = "Rank-based Ant System";  // src/RankBasedAntSystem.cu:10
+
+int fail(aco_colony *c, int status, const std::string &msg) {
+  if (c) c->err = msg;
+  return status;
+}
+
+int cuda_fail(aco_colony *c, cudaError_t e, const char *what) {
+  std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(c, ACO_ERR_OUT_OF_MEMORY, msg);
+  return fail(c, ACO_ERR_CUDA, msg);
+}
+
+#define ACO_CUDA(c, call, what)                          \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+template <class T>
+int dalloc(aco_colony *c, T **ptr, size_t count) {
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T) + 16);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+  c->allocations.push_back(p);
+  *ptr = static_cast<T *>(p);
+  return ACO_OK;
+}
+
+ColonyDev make_dev(const aco_colony *c) {
+  ColonyDev d;
+  d.n = c->n; d.m = c->m; d.K = c->K; d.ld = c->ld; d.ldk = c->ldk; d.ldm = c->ldm;
+  d.dist = c->dist; d.eta = c->eta; d.tau = c->tau; d.choice = c->choice;
+  d.nn = c->nn; d.eta_nn = c->eta_nn; d.tau_nn = c->tau_nn; d.choice_nn = c->choice_nn;
+  d.tours = c->tours; d.newlen = c->newlen; d.len = c->len;
+  d.succT = c->succT; d.predT = c->predT; d.gbtour = c->gbtour;
+  d.age = c->age; d.perf = c->perf; d.valid = c->valid; d.mean = c->mean;
+  d.dep_col = c->dep_col; d.dep_delta = c->dep_delta; d.st = c->st;
+  d.rho = c->p.rho; d.alpha = c->p.alpha; d.use_alpha = c->p.use_alpha;
+  d.aging = c->p.aging; d.min_ret = c->p.min_retirement_age;
+  d.max_ret = c->p.max_retirement_age; d.global_perf = c->p.global_performance;
+  d.min_pop = c->p.min_population_limit;
+  d.variant = c->p.variant; d.rank_w = c->p.rank_w; d.fallback = c->p.fallback;
+  d.seed = c->p.seed;
+  return d;
+}
+
+void drop_graph(aco_colony *c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = nullptr;
+  c->graph = nullptr;
+}
+
+int check_params(const aco_params *p, int n) {
+  if (!p || n < 3) return ACO_ERR_INVALID_ARGUMENT;
+  if (p->num_ants < 1 || p->num_ants > 65536) return ACO_ERR_INVALID_ARGUMENT;
+  if (n >= (1 << 21)) return ACO_ERR_UNSUPPORTED;
+  if (p->variant != ACO_ANT_SYSTEM && p->variant != ACO_RANK_BASED) return ACO_ERR_INVALID_ARGUMENT;
+  if (p->nn_order != ACO_NN_STABLE && p->nn_order != ACO_NN_REFERENCE_QSORT)
+    return ACO_ERR_INVALID_ARGUMENT;
+  if (p->heuristic != ACO_HEURISTIC_DEVICE && p->heuristic != ACO_HEURISTIC_LIBM)
+    return ACO_ERR_INVALID_ARGUMENT;
+  if (p->fallback != ACO_FALLBACK_REFERENCE && p->fallback != ACO_FALLBACK_BEST)
+    return ACO_ERR_INVALID_ARGUMENT;
+  if (p->deposit != ACO_DEPOSIT_DETERMINISTIC && p->deposit != ACO_DEPOSIT_ATOMIC)
+    return ACO_ERR_INVALID_ARGUMENT;
+  if (p->tau0_mode < ACO_TAU0_REFERENCE || p->tau0_mode > ACO_TAU0_VALUE)
+    return ACO_ERR_INVALID_ARGUMENT;
+  const int K = (p->cand_k <= 0 || p->cand_k >= n) ? n : p->cand_k;
+  if (K < n && p->fallback == ACO_FALLBACK_REFERENCE) return ACO_ERR_UNSUPPORTED;
+  if (p->nn_order == ACO_NN_STABLE && n > 16384) return ACO_ERR_UNSUPPORTED;
+  if (p->variant == ACO_RANK_BASED && p->rank_w < 1) return ACO_ERR_INVALID_ARGUMENT;
+  if (p->ants_per_block < 0 || p->ants_per_block > 16) return ACO_ERR_INVALID_ARGUMENT;
+  if (p->construct_mode < ACO_CONSTRUCT_AUTO || p->construct_mode > ACO_CONSTRUCT_STAGED)
+    return ACO_ERR_INVALID_ARGUMENT;
+  if (p->construct_mode == ACO_CONSTRUCT_STAGED && (K > 32 || n >= 32768))
+    return ACO_ERR_UNSUPPORTED;
+  return ACO_OK;
+}
+
+int allocate(aco_colony *c) {
+  const size_t n = c->n, m = c->m, ld = c->ld, ldk = c->ldk, ldm = c->ldm;
+  int s;
+  if ((s = dalloc(c, &c->dist, n * ld))) return s;
+  if ((s = dalloc(c, &c->eta, n * ld))) return s;
+  if ((s = dalloc(c, &c->tau, n * ld))) return s;
+  if ((s = dalloc(c, &c->choice, n * ld))) return s;
+  if ((s = dalloc(c, &c->nn, n * ldk))) return s;
+  if ((s = dalloc(c, &c->eta_nn, n * ldk))) return s;
+  if ((s = dalloc(c, &c->choice_nn, n * ldk))) return s;
+  if ((s = dalloc(c, &c->tau_nn, c->p.aging ? n * ldk : 32))) return s;
+  if ((s = dalloc(c, &c->tours, m * ld))) return s;
+  if ((s = dalloc(c, &c->newlen, m))) return s;
+  if ((s = dalloc(c, &c->len, m))) return s;
+  if ((s = dalloc(c, &c->succT, n * ldm))) return s;
+  if ((s = dalloc(c, &c->predT, n * ldm))) return s;
+  if ((s = dalloc(c, &c->gbtour, n))) return s;
+  if ((s = dalloc(c, &c->age, m))) return s;
+  if ((s = dalloc(c, &c->perf, m))) return s;
+  if ((s = dalloc(c, &c->valid, m))) return s;
+  if ((s = dalloc(c, &c->mean, ld))) return s;
+  if (c->K <= 32 && c->n < 32768)
+    if ((s = dalloc(c, &c->nn16, n * 32))) return s;
+  if ((s = dalloc(c, &c->dep_col, m + 1))) return s;
+  if ((s = dalloc(c, &c->dep_delta, m + 1))) return s;
+  if ((s = dalloc(c, &c->st, 1))) return s;
+  ACO_CUDA(c, cudaMemsetAsync(c->tours, 0, m * ld * 4, c->stream), "memset tours");
+  ACO_CUDA(c, cudaMemsetAsync(c->st, 0, sizeof(ColonyState), c->stream), "memset state");
+  ACO_CUDA(c, cudaMemsetAsync(c->gbtour, 0, n * 4, c->stream), "memset gbtour");
+  return ACO_OK;
+}
+
+int create_common(const aco_params *params, int32_t n, aco_colony **out, aco_colony **cp) {
+  if (!out) return ACO_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int s = check_params(params, n);
+  if (s) return s;
+  aco_colony *c = new (std::nothrow) aco_colony();
+  if (!c) return ACO_ERR_OUT_OF_MEMORY;
+  c->p = *params;
+  c->n = n;
+  c->m = params->num_ants;
+  c->K = (params->cand_k <= 0 || params->cand_k >= n) ? n : params->cand_k;
+  c->ld = round_up(n, 32);
+  c->ldk = round_up(c->K, 32);
+  c->ldm = round_up(c->m + 1, 32);
+  c->apb = params->ants_per_block > 0 ? params->ants_per_block : 4;
+  cudaGetDevice(&c->device);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  cudaDeviceGetAttribute(&c->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return ACO_ERR_CUDA;
+  }
+  c->own_stream = true;
+  for (int i = 0; i < 4; i++) cudaEventCreate(&c->ev[i]);
+  *cp = c;
+  if ((s = allocate(c))) {
+    aco_colony_destroy(c);
+    *cp = nullptr;
+    return s;
+  }
+  return ACO_OK;
+}
+
+int device_error(aco_colony *c) {
+  ColonyState h;
+  ACO_CUDA(c, cudaMemcpyAsync(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost, c->stream),
+           "read state");
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  if (h.error & kErrTimeout) return fail(c, ACO_ERR_DEVICE_TIMEOUT, "a bounded device wait expired");
+  if (h.error & kErrCheck) return fail(c, ACO_ERR_DEVICE_CHECK, "a device-side check failed");
+  return ACO_OK;
+}
+
+int read_state(aco_colony *c, ColonyState *h) {
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  ACO_CUDA(c, cudaMemcpyAsync(h, c->st, sizeof(*h), cudaMemcpyDeviceToHost, c->stream),
+           "read state");
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  return ACO_OK;
+}
+
+cudaError_t launch_construction(aco_colony *c, const ColonyDev &d) {
+  if (c->staged)
+    return launch_construct_staged(d, c->nn16, c->staged_grid, c->staged_warps, c->stream);
+  return launch_construct(d, c->apb, c->stream);
+}
+
+// Chooses between the staged kernel (whole candidate table in shared
+// memory, one CTA per SM) and the global-memory kernel.
+int plan_construction(aco_colony *c) {
+  c->staged = false;
+  if (c->K > 32 || c->n >= 32768 || !c->nn16 || c->p.construct_mode == ACO_CONSTRUCT_GLOBAL)
+    return ACO_OK;
+  const int sms = c->num_sms > 0 ? c->num_sms : 1;
+  int warps = (c->m + sms - 1) / sms;
+  warps = warps < 1 ? 1 : (warps > 32 ? 32 : warps);
+  const size_t smem = construct_staged_smem_bytes(c->n, c->ld, c->p.aging != 0, warps);
+  if (smem > (size_t)c->max_smem_optin) {
+    if (c->p.construct_mode == ACO_CONSTRUCT_STAGED)
+      return fail(c, ACO_ERR_UNSUPPORTED, "candidate table does not fit in shared memory");
+    return ACO_OK;
+  }
+  ACO_CUDA(c, configure_construct_staged(smem), "configure staged construct");
+  c->staged = true;
+  c->staged_warps = warps;
+  c->staged_grid = (c->m + warps - 1) / warps;
+  if (c->staged_grid > sms) c->staged_grid = sms;
+  return ACO_OK;
+}
+
+int enqueue_iteration(aco_colony *c) {
+  const ColonyDev d = make_dev(c);
+  ACO_CUDA(c, launch_construction(c, d), "construct");
+  ACO_CUDA(c, launch_epilogue(d, c->stream), "epilogue");
+  if (c->p.deposit == ACO_DEPOSIT_ATOMIC) {
+    ACO_CUDA(c, launch_evaporate(d, c->stream), "evaporate");
+    ACO_CUDA(c, launch_deposit_atomic(d, c->stream), "deposit");
+    ACO_CUDA(c, launch_pheromone_rows(d, false, false, false, c->stream), "choice rows");
+    c->launches += 5;
+  } else {
+    ACO_CUDA(c, launch_pheromone_rows(d, true, true, true, c->stream), "pheromone rows");
+    c->launches += 3;
+  }
+  return ACO_OK;
+}
+
+int read_matrix_f32(aco_colony *c, const float *src, int cols, int ldsrc, float *out) {
+  if (!out) return fail(c, ACO_ERR_INVALID_ARGUMENT, "null output");
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  ACO_CUDA(c, cudaMemcpy2DAsync(out, (size_t)cols * 4, src, (size_t)ldsrc * 4, (size_t)cols * 4,
+                                c->n, cudaMemcpyDeviceToHost, c->stream),
+           "read matrix");
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  return ACO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void aco_params_default(aco_params *p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->variant = ACO_ANT_SYSTEM;
+  p->num_ants = 10;      // DEFAULT_NUM_ANTS
+  p->alpha = 1.0f;       // DEFAULT_ALPHA
+  p->beta = 5.0f;        // DEFAULT_BETA
+  p->rho = 0.1f;         // DEFAULT_RHO
+  p->use_alpha = 0;
+  p->cand_k = 0;
+  p->nn_order = ACO_NN_REFERENCE_QSORT;
+  p->heuristic = ACO_HEURISTIC_LIBM;
+  p->fallback = ACO_FALLBACK_REFERENCE;
+  p->deposit = ACO_DEPOSIT_DETERMINISTIC;
+  p->tau0_mode = ACO_TAU0_REFERENCE;
+  p->tau0 = 1e-6f;
+  p->rank_w = 5;         // DEFAULT_NUM_RANK_ANTS
+  p->aging = 0;
+  p->min_retirement_age = 30;
+  p->max_retirement_age = 50;
+  p->local_performance = 10;
+  p->global_performance = 10;
+  p->min_population_limit = 40;
+  p->max_population_limit = 100;
+  p->seed = 12345678;    // RANDOM_SEED, inc/Colony.h:15
+}
+
+int aco_colony_create(const aco_params *params, const int32_t *dist, int32_t n,
+                      int32_t dist_on_device, aco_colony **out) {
+  if (!dist) return ACO_ERR_INVALID_ARGUMENT;
+  aco_colony *c = nullptr;
+  int s = create_common(params, n, out, &c);
+  if (s) return s;
+  const cudaMemcpyKind kind = dist_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  cudaError_t e = cudaMemcpy2DAsync(c->dist, (size_t)c->ld * 4, dist, (size_t)n * 4,
+                                    (size_t)n * 4, n, kind, c->stream);
+  if (e == cudaSuccess) e = launch_fill_padding_int(c->dist, n, c->ld, ACO_MAX_DISTANCE, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    aco_colony_destroy(c);
+    return ACO_ERR_CUDA;
+  }
+  *out = c;
+  return ACO_OK;
+}
+
+int aco_colony_create_coords(const aco_params *params, const float *x, const float *y, int32_t n,
+                             aco_colony **out) {
+  if (!x || !y) return ACO_ERR_INVALID_ARGUMENT;
+  aco_colony *c = nullptr;
+  int s = create_common(params, n, out, &c);
+  if (s) return s;
+  float *dxy = nullptr;
+  cudaError_t e = cudaMallocAsync(&dxy, (size_t)2 * n * 4, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dxy, x, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dxy + n, y, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = launch_distances_from_coords(dxy, dxy + n, n, c->ld, c->dist, c->stream);
+  if (dxy) cudaFreeAsync(dxy, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    aco_colony_destroy(c);
+    return ACO_ERR_CUDA;
+  }
+  *out = c;
+  return ACO_OK;
+}
+
+int aco_colony_initialize(aco_colony *c) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  drop_graph(c);
+  c->initialized = false;
+  const int n = c->n;
+  // RankBasedAntSystem::computeParameters (src/RankBasedAntSystem.cu:31-36)
+  if (c->p.variant == ACO_RANK_BASED && c->p.rank_w > n) c->p.rank_w = n;
+  ACO_CUDA(c, cudaMemsetAsync(c->st, 0, sizeof(ColonyState), c->stream), "reset state");
+
+  // heuristic (Colony::computeHurestics, src/Colony.cu:232-246)
+  if (c->p.heuristic == ACO_HEURISTIC_DEVICE) {
+    ACO_CUDA(c, launch_heuristic_device(c->dist, n, c->ld, c->p.beta, c->eta, c->stream),
+             "heuristic");
+  } else {
+    int32_t *dmax = nullptr;
+    ACO_CUDA(c, cudaMallocAsync(&dmax, 4, c->stream), "alloc");
+    ACO_CUDA(c, cudaMemsetAsync(dmax, 0, 4, c->stream), "memset");
+    ACO_CUDA(c, launch_max_distance(c->dist, n, c->ld, dmax, c->stream), "max distance");
+    int32_t hmax = 0;
+    ACO_CUDA(c, cudaMemcpyAsync(&hmax, dmax, 4, cudaMemcpyDeviceToHost, c->stream), "read max");
+    ACO_CUDA(c, cudaFreeAsync(dmax, c->stream), "free");
+    ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+    if (hmax < 0 || hmax >= (1 << 26))
+      return fail(c, ACO_ERR_UNSUPPORTED, "distances too large for the libm heuristic table");
+    // HURESTIC(d, beta) of the reference CPU build (inc/Colony.h:20), one
+    // entry per distinct distance value.
+    std::vector<float> table((size_t)hmax + 1);
+    for (int32_t d = 0; d <= hmax; d++) table[d] = powf((float)(1.0 / ((float)d)), c->p.beta);
+    float *dtab = nullptr;
+    ACO_CUDA(c, cudaMallocAsync(&dtab, table.size() * 4, c->stream), "alloc table");
+    ACO_CUDA(c, cudaMemcpyAsync(dtab, table.data(), table.size() * 4, cudaMemcpyHostToDevice,
+                                c->stream),
+             "upload table");
+    ACO_CUDA(c, launch_heuristic_table(c->dist, n, c->ld, dtab, hmax + 1, c->eta, c->st, c->stream),
+             "heuristic table");
+    ACO_CUDA(c, cudaFreeAsync(dtab, c->stream), "free table");
+    ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  }
+
+  // nn-list (Colony::computeNNlist, src/Colony.cu:276-311)
+  if (c->p.nn_order == ACO_NN_STABLE) {
+    ACO_CUDA(c, launch_nn_sort_stable(c->dist, n, c->ld, c->K, c->ldk, c->nn, c->st, c->stream),
+             "nn sort");
+  } else {
+    int32_t *scratch = nullptr, *full = nullptr;
+    ACO_CUDA(c, cudaMallocAsync(&scratch, (size_t)n * c->ld * 4, c->stream), "alloc scratch");
+    if (c->K == n) {
+      full = c->nn;
+    } else {
+      ACO_CUDA(c, cudaMallocAsync(&full, (size_t)n * c->ld * 4, c->stream), "alloc scratch");
+    }
+    ACO_CUDA(c, launch_nn_ref_qsort(c->dist, n, c->ld, scratch, full, c->K == n ? c->ldk : c->ld,
+                                    c->st, c->stream),
+             "nn quicksort");
+    if (full != c->nn) {
+      ACO_CUDA(c, cudaMemsetAsync(c->nn, 0xff, (size_t)n * c->ldk * 4, c->stream), "memset nn");
+      ACO_CUDA(c, cudaMemcpy2DAsync(c->nn, (size_t)c->ldk * 4, full, (size_t)c->ld * 4,
+                                    (size_t)c->K * 4, n, cudaMemcpyDeviceToDevice, c->stream),
+               "copy nn");
+      ACO_CUDA(c, cudaFreeAsync(full, c->stream), "free");
+    }
+    ACO_CUDA(c, cudaFreeAsync(scratch, c->stream), "free");
+  }
+  ACO_CUDA(c, launch_gather_nn_f32(c->eta, n, c->ld, c->nn, c->K, c->ldk, c->eta_nn, c->stream),
+           "eta_nn");
+  if (c->nn16) ACO_CUDA(c, launch_nn_to_i16(c->nn, n, c->ldk, c->nn16, c->stream), "nn16");
+
+  const ColonyDev d = make_dev(c);
+  ACO_CUDA(c, launch_greedy_tau0(d, c->p.tau0_mode, c->p.tau0, c->stream), "tau0");
+  ACO_CUDA(c, launch_init_colony(d, c->stream), "init");
+  ACO_CUDA(c, configure_construct(construct_smem_bytes(n, c->K, c->apb)), "configure construct");
+  ACO_CUDA(c, configure_pheromone_rows(c->ld), "configure rows");
+  if (int s0 = plan_construction(c)) return s0;
+  ACO_CUDA(c, launch_pheromone_rows(d, false, false, false, c->stream), "choice rows");
+  int s = device_error(c);
+  if (s) return s;
+  c->initialized = true;
+  return ACO_OK;
+}
+
+int aco_colony_construct_solution(aco_colony *c, float *timers_ms) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  if (!timers_ms) return enqueue_iteration(c);
+  const ColonyDev d = make_dev(c);
+  ACO_CUDA(c, cudaEventRecord(c->ev[0], c->stream), "event");
+  ACO_CUDA(c, launch_construction(c, d), "construct");
+  ACO_CUDA(c, cudaEventRecord(c->ev[1], c->stream), "event");
+  ACO_CUDA(c, launch_epilogue(d, c->stream), "epilogue");
+  ACO_CUDA(c, cudaEventRecord(c->ev[2], c->stream), "event");
+  if (c->p.deposit == ACO_DEPOSIT_ATOMIC) {
+    ACO_CUDA(c, launch_evaporate(d, c->stream), "evaporate");
+    ACO_CUDA(c, launch_deposit_atomic(d, c->stream), "deposit");
+    ACO_CUDA(c, launch_pheromone_rows(d, false, false, false, c->stream), "choice rows");
+    c->launches += 5;
+  } else {
+    ACO_CUDA(c, launch_pheromone_rows(d, true, true, true, c->stream), "pheromone rows");
+    c->launches += 3;
+  }
+  ACO_CUDA(c, cudaEventRecord(c->ev[3], c->stream), "event");
+  ACO_CUDA(c, cudaEventSynchronize(c->ev[3]), "synchronize");
+  float t[3];
+  for (int i = 0; i < 3; i++) cudaEventElapsedTime(&t[i], c->ev[i], c->ev[i + 1]);
+  for (int i = 0; i < ACO_TOTAL_TIMERS; i++) timers_ms[i] = 0.0f;
+  // initTour and the choice-info are fused into construction and into the
+  // pheromone pass; their slots stay 0.
+  timers_ms[ACO_TIME_TOUR] = t[0];
+  timers_ms[ACO_TIME_COMPUTE_ANT_DISTANCE] = t[1];
+  timers_ms[ACO_TIME_UPDATE_PHEROMONE] = t[2];
+  return device_error(c);
+}
+
+int aco_colony_run(aco_colony *c, int32_t iterations) {
+  if (!c || iterations < 0) return ACO_ERR_INVALID_ARGUMENT;
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  if (iterations == 0) return ACO_OK;
+  if (!c->graph_exec) {
+    const int64_t before = c->launches;
+    ACO_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture");
+    int s = enqueue_iteration(c);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (s) {
+      if (g) cudaGraphDestroy(g);
+      return s;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "end capture");
+    c->graph = g;
+    ACO_CUDA(c, cudaGraphInstantiate(&c->graph_exec, g, 0), "instantiate");
+    c->launches = before;  // capture itself launches nothing
+  }
+  const int per_iter = c->p.deposit == ACO_DEPOSIT_ATOMIC ? 5 : 3;
+  for (int32_t i = 0; i < iterations; i++)
+    ACO_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream), "graph launch");
+  c->launches += (int64_t)per_iter * iterations;
+  return ACO_OK;
+}
+
+int aco_colony_synchronize(aco_colony *c) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  return device_error(c);
+}
+
+int aco_colony_get_iter_best(aco_colony *c, int64_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  ColonyState h;
+  int s = read_state(c, &h);
+  if (!s) *out = h.iter_best;
+  return s;
+}
+
+int aco_colony_get_glob_best(aco_colony *c, int64_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  ColonyState h;
+  int s = read_state(c, &h);
+  if (!s) *out = h.glob_best;
+  return s;
+}
+
+int aco_colony_get_num_valid_ants(aco_colony *c, int32_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  if (!c->p.aging) {  // Colony::getNumValidAnts, src/Colony.cu:464-466
+    *out = c->m;
+    return ACO_OK;
+  }
+  ColonyState h;
+  int s = read_state(c, &h);
+  if (!s) *out = h.num_valid;
+  return s;
+}
+
+int aco_colony_get_iteration(aco_colony *c, int32_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  ColonyState h;
+  int s = read_state(c, &h);
+  if (!s) *out = (int32_t)h.iteration;
+  return s;
+}
+
+int aco_colony_get_reps(aco_colony *c, int32_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  *out = 0;  // reps is never incremented by the reference (src/Colony.cu:35)
+  return ACO_OK;
+}
+
+int aco_colony_get_size(aco_colony *c, int32_t *n, int32_t *m, int32_t *k) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  if (n) *n = c->n;
+  if (m) *m = c->m;
+  if (k) *k = c->K;
+  return ACO_OK;
+}
+
+int aco_colony_get_params(aco_colony *c, aco_params *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  *out = c->p;
+  return ACO_OK;
+}
+
+int aco_colony_set_alpha(aco_colony *c, float v) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  c->p.alpha = v;
+  drop_graph(c);
+  return ACO_OK;
+}
+
+int aco_colony_set_beta(aco_colony *c, float v) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  c->p.beta = v;
+  return ACO_OK;
+}
+
+int aco_colony_set_rho(aco_colony *c, float v) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  c->p.rho = v;
+  drop_graph(c);
+  return ACO_OK;
+}
+
+int aco_colony_set_optimum(aco_colony *c, int64_t v) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  c->optimum = v;
+  return ACO_OK;
+}
+
+int aco_colony_set_rank_w(aco_colony *c, int32_t w) {
+  if (!c || w < 1) return ACO_ERR_INVALID_ARGUMENT;
+  c->p.rank_w = w;
+  drop_graph(c);
+  return ACO_OK;
+}
+
+int aco_colony_set_aging_params(aco_colony *c, const int32_t six[6]) {
+  if (!c || !six) return ACO_ERR_INVALID_ARGUMENT;
+  c->p.min_retirement_age = six[0];
+  c->p.max_retirement_age = six[1];
+  c->p.local_performance = six[2];
+  c->p.global_performance = six[3];
+  c->p.min_population_limit = six[4];
+  c->p.max_population_limit = six[5];
+  drop_graph(c);
+  return ACO_OK;
+}
+
+const char *aco_colony_name(const aco_colony *c) {
+  if (!c) return "";
+  return c->p.variant == ACO_RANK_BASED ? kNameRBAS : kNameAS;
+}
+
+int aco_colony_get_best_tour(aco_colony *c, int32_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  ACO_CUDA(c, cudaMemcpyAsync(out, c->gbtour, (size_t)c->n * 4, cudaMemcpyDeviceToHost, c->stream),
+           "read best tour");
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  return ACO_OK;
+}
+
+int aco_colony_read_pheromone(aco_colony *c, float *out) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  return read_matrix_f32(c, c->tau, c->n, c->ld, out);
+}
+
+int aco_colony_write_pheromone(aco_colony *c, const float *in) {
+  if (!c || !in) return ACO_ERR_INVALID_ARGUMENT;
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  ACO_CUDA(c, cudaMemcpy2DAsync(c->tau, (size_t)c->ld * 4, in, (size_t)c->n * 4, (size_t)c->n * 4,
+                                c->n, cudaMemcpyHostToDevice, c->stream),
+           "write pheromone");
+  ACO_CUDA(c, launch_pheromone_rows(make_dev(c), false, false, false, c->stream), "choice rows");
+  return device_error(c);
+}
+
+int aco_colony_read_heuristic(aco_colony *c, float *out) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  return read_matrix_f32(c, c->eta, c->n, c->ld, out);
+}
+
+int aco_colony_read_choice_info(aco_colony *c, float *out) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  return read_matrix_f32(c, c->choice, c->n, c->ld, out);
+}
+
+int aco_colony_read_nn_list(aco_colony *c, int32_t *out) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  return read_matrix_f32(c, reinterpret_cast<const float *>(c->nn), c->K, c->ldk,
+                         reinterpret_cast<float *>(out));
+}
+
+int aco_colony_read_distances(aco_colony *c, int32_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  ACO_CUDA(c, cudaMemcpy2DAsync(out, (size_t)c->n * 4, c->dist, (size_t)c->ld * 4,
+                                (size_t)c->n * 4, c->n, cudaMemcpyDeviceToHost, c->stream),
+           "read distances");
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  return ACO_OK;
+}
+
+int aco_colony_read_tours(aco_colony *c, int32_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  ACO_CUDA(c, cudaMemcpy2DAsync(out, (size_t)c->n * 4, c->tours, (size_t)c->ld * 4,
+                                (size_t)c->n * 4, c->m, cudaMemcpyDeviceToHost, c->stream),
+           "read tours");
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  return ACO_OK;
+}
+
+int aco_colony_read_tour_lengths(aco_colony *c, int64_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  ACO_CUDA(c, cudaMemcpyAsync(out, c->len, (size_t)c->m * 8, cudaMemcpyDeviceToHost, c->stream),
+           "read lengths");
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  return ACO_OK;
+}
+
+int aco_colony_read_aging(aco_colony *c, int32_t *age, int32_t *perf, uint8_t *valid, float *mean,
+                          int32_t *misc) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  ColonyState h;
+  int s = read_state(c, &h);
+  if (s) return s;
+  if (age) ACO_CUDA(c, cudaMemcpy(age, c->age, (size_t)c->m * 4, cudaMemcpyDeviceToHost), "read");
+  if (perf) ACO_CUDA(c, cudaMemcpy(perf, c->perf, (size_t)c->m * 4, cudaMemcpyDeviceToHost), "read");
+  if (valid) ACO_CUDA(c, cudaMemcpy(valid, c->valid, (size_t)c->m, cudaMemcpyDeviceToHost), "read");
+  if (mean) ACO_CUDA(c, cudaMemcpy(mean, c->mean, (size_t)c->n * 4, cudaMemcpyDeviceToHost), "read");
+  if (misc) {
+    misc[0] = h.isconverged;
+    misc[1] = h.globalperformance;
+  }
+  return ACO_OK;
+}
+
+int aco_colony_get_stats(aco_colony *c, aco_stats *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  ColonyState h;
+  int s = read_state(c, &h);
+  if (s) return s;
+  memset(out, 0, sizeof(*out));
+  out->iteration = h.iteration;
+  out->tours_built = h.tours_built;
+  out->fallbacks = h.fallbacks;
+  out->greedy_length = h.greedy_length;
+  out->iter_best = h.iter_best;
+  out->glob_best = h.glob_best;
+  out->num_valid = c->p.aging ? h.num_valid : c->m;
+  out->tau0 = h.tau0;
+  return ACO_OK;
+}
+
+int aco_colony_set_stream(aco_colony *c, void *stream) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  c->stream = static_cast<cudaStream_t>(stream);
+  c->own_stream = false;
+  drop_graph(c);
+  return ACO_OK;
+}
+
+int aco_colony_get_launch_count(aco_colony *c, int64_t *out) {
+  if (!c || !out) return ACO_ERR_INVALID_ARGUMENT;
+  *out = c->launches;
+  return ACO_OK;
+}
+
+const char *aco_colony_last_error(const aco_colony *c) { return c ? c->err.c_str() : ""; }
+
+const char *aco_status_string(int status) {
+  switch (status) {
+    case ACO_OK: return "ok";
+    case ACO_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case ACO_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case ACO_ERR_CUDA: return "CUDA error";
+    case ACO_ERR_NOT_INITIALIZED: return "not initialized";
+    case ACO_ERR_UNSUPPORTED: return "unsupported configuration";
+    case ACO_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+    case ACO_ERR_DEVICE_CHECK: return "device check failed";
+    default: return "unknown status";
+  }
+}
+
+void aco_colony_destroy(aco_colony *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
+  for (void *p : c->allocations) cudaFree(p);
+  for (int i = 0; i < 4; i++)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+}  // extern "C"

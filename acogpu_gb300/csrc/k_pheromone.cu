@@ -1,0 +1,244 @@
+// k_pheromone.cu -- pheromone evaporation + deposit, fused with the next
+// iteration's choice-info.
+//
+// Deterministic mode (the default): one CTA owns row j of tau.  It stages
+// the tau row and the eta row in shared memory with TMA bulk copies,
+// evaporates (AntSystem::evaporatePheromones, src/AntSystem.cu:218-223:
+// tau = max((1 - rho) tau, 1e-18)), then applies the deposit list in order.
+// The edges that touch row j are already bucketed by row (succT/predT[j][k]
+// written by construction), so the row's deposits are a segmented fold: each
+// element receives its +delta_k in ascending ant order, exactly the float
+// sequence of the reference's sequential update (src/AntSystem.cu:296-316),
+// which mirrors tau[j][h] into tau[h][j].  Within a chunk of 32 ants, lanes
+// that hit the same element are grouped through a shared-memory mask table
+// and the lowest lane folds the group in lane order.
+//
+// After the update the same CTA writes choice = tau * eta (the noaging
+// fitness, inc/Colony.cuh:29-30; the reference's dev_compute_selection,
+// inc/Colony.cuh:91-99), choice and tau in candidate order, and for aging the
+// row mean of Colony::computePheromoneMean (src/Colony.cu:435-441), a
+// sequential float sum.
+//
+// Atomic mode: a float4 evaporation pass, then one red.global.add.f32 per
+// directed edge, then the same row pass without evaporation or deposit.
+#include <cuda_runtime.h>
+
+#include "aco_kernels.h"
+
+namespace aco {
+
+constexpr int kRowThreads = 256;
+
+__device__ __forceinline__ float choice_of(float tau, float eta, int use_alpha, float alpha) {
+  const float p = use_alpha ? powf(tau, alpha) : tau;
+  return __fmul_rn(p, eta);
+}
+
+template <bool EVAP, bool DEPOSIT, bool WRITE_TAU>
+__global__ void __launch_bounds__(kRowThreads) k_pheromone_rows(ColonyDev c) {
+  extern __shared__ __align__(128) unsigned char smem_rows[];
+  const int ld = c.ld, n = c.n, tid = threadIdx.x, j = blockIdx.x;
+  float *row = reinterpret_cast<float *>(smem_rows);
+  float *erow = row + ld;
+  uint32_t *mt = reinterpret_cast<uint32_t *>(erow + ld);
+  float *dl = reinterpret_cast<float *>(mt + (DEPOSIT ? ld : 0));
+  uint64_t *bar = reinterpret_cast<uint64_t *>(dl + 32);
+  int *flag = reinterpret_cast<int *>(bar + 1);
+
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_barrier_init();
+  }
+  if (DEPOSIT)
+    for (int h = tid; h < ld; h += kRowThreads) mt[h] = 0;
+  __syncthreads();
+  if (tid == 0) {
+    const uint32_t bytes = (uint32_t)ld * 4u;
+    mbar_arrive_expect_tx(bar, 2u * bytes);
+    tma_load_1d(row, c.tau + (size_t)j * ld, bytes, bar);
+    tma_load_1d(erow, c.eta + (size_t)j * ld, bytes, bar);
+    *flag = mbar_wait_bounded(bar, 0, c.st) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!*flag) return;
+
+  if (EVAP) {
+    const float keep = __fsub_rn(1.0f, c.rho);
+    const float fmin = min_pheromone();
+    for (int h = tid; h < n; h += kRowThreads) {
+      const float v = __fmul_rn(keep, row[h]);
+      row[h] = v > fmin ? v : fmin;
+    }
+    __syncthreads();
+  }
+
+  if (DEPOSIT) {
+    if (tid < 32) {
+      const int lane = tid;
+      const int cnt = c.st->dep_count;
+      const size_t base_row = (size_t)j * c.ldm;
+      for (int base = 0; base < cnt; base += 32) {
+        const int q = base + lane;
+        int col = -1;
+        float d = 0.0f;
+        if (q < cnt) {
+          col = c.dep_col[q];
+          d = c.dep_delta[q];
+        }
+        int sN = -1, pN = -1;
+        if (col >= 0) {
+          sN = c.succT[base_row + col];
+          pN = c.predT[base_row + col];
+          if ((unsigned)sN >= (unsigned)n || (unsigned)pN >= (unsigned)n) {
+            atomicOr(&c.st->error, kErrCheck);
+            sN = pN = -1;
+          }
+        }
+        dl[lane] = d;
+        if (sN >= 0) atomicOr(&mt[sN], 1u << lane);
+        if (pN >= 0) atomicOr(&mt[pN], 1u << lane);
+        __syncwarp();
+        if (sN >= 0) {
+          unsigned M = mt[sN];
+          if (__ffs(M) - 1 == lane) {
+            float v = row[sN];
+            while (M) {
+              const int b = __ffs(M) - 1;
+              M &= M - 1;
+              v = __fadd_rn(v, dl[b]);
+            }
+            row[sN] = v;
+          }
+        }
+        if (pN >= 0) {
+          unsigned M = mt[pN];
+          if (__ffs(M) - 1 == lane) {
+            float v = row[pN];
+            while (M) {
+              const int b = __ffs(M) - 1;
+              M &= M - 1;
+              v = __fadd_rn(v, dl[b]);
+            }
+            row[pN] = v;
+          }
+        }
+        __syncwarp();
+        if (sN >= 0) mt[sN] = 0;
+        if (pN >= 0) mt[pN] = 0;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+  }
+
+  float *trow = c.tau + (size_t)j * ld;
+  float *crow = c.choice + (size_t)j * ld;
+  for (int h4 = tid; h4 < ld / 4; h4 += kRowThreads) {
+    const float4 t = reinterpret_cast<const float4 *>(row)[h4];
+    const float4 e = reinterpret_cast<const float4 *>(erow)[h4];
+    if (WRITE_TAU) reinterpret_cast<float4 *>(trow)[h4] = t;
+    float4 cv;
+    cv.x = choice_of(t.x, e.x, c.use_alpha, c.alpha);
+    cv.y = choice_of(t.y, e.y, c.use_alpha, c.alpha);
+    cv.z = choice_of(t.z, e.z, c.use_alpha, c.alpha);
+    cv.w = choice_of(t.w, e.w, c.use_alpha, c.alpha);
+    reinterpret_cast<float4 *>(crow)[h4] = cv;
+  }
+  const size_t koff = (size_t)j * c.ldk;
+  for (int r = tid; r < c.ldk; r += kRowThreads) {
+    float cv = 0.0f, tv = 0.0f;
+    if (r < c.K) {
+      const int id = c.nn[koff + r];
+      tv = row[id];
+      cv = choice_of(tv, erow[id], c.use_alpha, c.alpha);
+    }
+    c.choice_nn[koff + r] = cv;
+    if (c.aging) c.tau_nn[koff + r] = tv;
+  }
+  if (c.aging && tid == 0) {
+    float s = 0.0f;
+    for (int h = 0; h < n; h++) s = __fadd_rn(s, row[h]);
+    c.mean[j] = __fdiv_rn(s, __int2float_rn(n));
+  }
+}
+
+static size_t rows_smem(int ld, bool deposit) {
+  return (size_t)ld * 4 * (deposit ? 3 : 2) + 32 * 4 + 16;
+}
+
+template <bool EVAP, bool DEPOSIT, bool WRITE_TAU>
+static cudaError_t launch_rows_t(const ColonyDev &c, cudaStream_t s) {
+  const size_t smem = rows_smem(c.ld, DEPOSIT);
+  k_pheromone_rows<EVAP, DEPOSIT, WRITE_TAU><<<c.n, kRowThreads, smem, s>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t configure_pheromone_rows(int ld) {
+  const int a = (int)rows_smem(ld, false), b = (int)rows_smem(ld, true);
+  cudaError_t e = cudaFuncSetAttribute(k_pheromone_rows<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pheromone_rows<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pheromone_rows<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pheromone_rows<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pheromone_rows<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a);
+  return e;
+}
+
+cudaError_t launch_pheromone_rows(const ColonyDev &c, bool evaporate, bool deposit,
+                                  bool write_tau, cudaStream_t s) {
+  if (evaporate && deposit) return launch_rows_t<true, true, true>(c, s);
+  if (evaporate) return launch_rows_t<true, false, true>(c, s);
+  if (deposit) return launch_rows_t<false, true, true>(c, s);
+  return write_tau ? launch_rows_t<false, false, true>(c, s)
+                   : launch_rows_t<false, false, false>(c, s);
+}
+
+// ---------------------------------------------------------------- atomic mode
+__global__ void k_evaporate(float *__restrict__ tau, int64_t total4, float rho) {
+  const float keep = __fsub_rn(1.0f, rho);
+  const float fmin = min_pheromone();
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    float4 v = reinterpret_cast<float4 *>(tau)[t];
+    v.x = __fmul_rn(keep, v.x);
+    v.y = __fmul_rn(keep, v.y);
+    v.z = __fmul_rn(keep, v.z);
+    v.w = __fmul_rn(keep, v.w);
+    v.x = v.x > fmin ? v.x : fmin;
+    v.y = v.y > fmin ? v.y : fmin;
+    v.z = v.z > fmin ? v.z : fmin;
+    v.w = v.w > fmin ? v.w : fmin;
+    reinterpret_cast<float4 *>(tau)[t] = v;
+  }
+}
+
+cudaError_t launch_evaporate(const ColonyDev &c, cudaStream_t s) {
+  k_evaporate<<<4 * 152, 256, 0, s>>>(c.tau, (int64_t)c.n * c.ld / 4, c.rho);
+  return cudaGetLastError();
+}
+
+// One thread per (deposit entry, tour position): both directions of the
+// edge receive +delta (the reference's GPU kernel updated one direction
+// only, src/AntSystem.cu:105-128; its CPU path is symmetric).
+__global__ void k_deposit_atomic(ColonyDev c) {
+  const int n = c.n;
+  const int cnt = c.st->dep_count;
+  const int64_t total = (int64_t)cnt * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(t / n), i = (int)(t % n);
+    const int col = c.dep_col[q];
+    if (col < 0) continue;
+    const int32_t *tour = col < c.m ? c.tours + (size_t)col * c.ld : c.gbtour;
+    const int a = tour[i], b = tour[i + 1 == n ? 0 : i + 1];
+    const float d = c.dep_delta[q];
+    atomicAdd(c.tau + (size_t)a * c.ld + b, d);
+    atomicAdd(c.tau + (size_t)b * c.ld + a, d);
+  }
+}
+
+cudaError_t launch_deposit_atomic(const ColonyDev &c, cudaStream_t s) {
+  k_deposit_atomic<<<8 * 152, 256, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
+}  // namespace aco

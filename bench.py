@@ -1,0 +1,329 @@
+"""Throughput benchmark of the GB300 ACO engine.
+
+Workload (one "step" = one full iteration of the hot path: construction of
+every ant's tour, tour lengths and bests, evaporation + deposit, next
+choice-info): rank-based Ant System with ant aging, n = 1000 cities drawn
+from 20 Gaussian clusters (sigma 300) in [0,10000)^2, m = 1000 ants, w = 6,
+candidate lists k = 30, rho = 0.1, FP32 pheromone, deterministic deposit.
+Synthetic seeded instance (no TSPLIB file is read).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is tours/s over the device-timed
+steps (CUDA events on the colony's stream, L2 flushed between steps);
+`e2e` is the same metric through the public API from host buffers, the way
+the reference's TSP::execute drives a colony (create from the host distance
+matrix, initialize, per step constructSolution + the three getters, final
+getTour).  With --gpus N > 1 every rank runs an independent replica (the
+single-instance path does not shard; replicas only).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CITIES, N_ANTS, RANK_W, CAND_K, RHO, BETA = 1000, 1000, 6, 30, 0.1, 2.0
+INSTANCE_SEED = 2026
+WORKLOAD = ("rank-based Ant System with aging, n=1000 (20 Gaussian clusters, sigma 300, "
+            "[0,10000)^2), m=1000, w=6, k=30, rho=0.1")
+L2_FLUSH_BYTES = 256 << 20
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def workload_params():
+    from acogpu_gb300 import _abi
+    return _abi.default_params(
+        num_ants=N_ANTS, variant=_abi.ACO_RANK_BASED, rank_w=RANK_W, aging=1, cand_k=CAND_K,
+        rho=RHO, beta=BETA, nn_order=_abi.ACO_NN_STABLE, heuristic=_abi.ACO_HEURISTIC_DEVICE,
+        fallback=_abi.ACO_FALLBACK_BEST, tau0_mode=_abi.ACO_TAU0_DORIGO,
+        deposit=_abi.ACO_DEPOSIT_DETERMINISTIC, seed=1234)
+
+
+def workload_instance():
+    from acogpu_gb300 import instances
+    x, y = instances.clustered_instance(N_CITIES, seed=INSTANCE_SEED)
+    return x, y, instances.euc2d_distances(x, y)
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={CLOCK_FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [v.strip() for v in line.split(",")]
+                if len(f) >= 9 and f[1].isdigit():
+                    rows.append(f)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [int(r[1]) for r in rows]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = [nm for i, nm in enumerate(names) if any(r[5 + i] == "Active" for r in rows)]
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": int(rows[0][2]),
+                "samples": len(rows), "reasons": reasons}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def construct_bytes(n, k, tours, fallbacks):
+    """Algorithmic bytes of the construction kernel: per ant-step the k
+    candidate ids and k choice weights (8k), the tour write and the distance
+    lookup (8); per fallback step one full choice row (4n)."""
+    return tours * (n - 1) * (8 * k + 8) + fallbacks * 4 * n
+
+
+def cpu_baseline(steps_iters=2):
+    """The CPU oracle on this host's cores, same algorithm and instance as
+    the GPU run, a bounded sample of iterations."""
+    import oracle
+    x, y, d = workload_instance()
+    threads = os.cpu_count() or 1
+    q = oracle.Port(workload_params(), d, threads=threads)
+    q.initialize()
+    q.iterate(1)
+    t0 = time.perf_counter()
+    q.iterate(steps_iters)
+    dt = time.perf_counter() - t0
+    tours = steps_iters * q.num_valid()
+    q.close()
+    return {"value": tours / dt, "unit": "tours/s", "cores": threads, "kind": "port",
+            "sample": f"{steps_iters} iterations of the same workload (after 1 warm-up) with the "
+                      f"C oracle, construction spread over {threads} threads"}
+
+
+def run_reference(args, rank):
+    """Reference arm: the reference's CPU algorithm (full-row roulette, its
+    only construction rule; AS update, its rank-based update is an empty
+    stub), restated in C, on the host cores, same instance and ant count."""
+    if rank != 0:
+        return None
+    import oracle
+    from acogpu_gb300 import _abi
+    x, y, d = workload_instance()
+    p = _abi.default_params(num_ants=N_ANTS, aging=1, rho=RHO, beta=BETA, cand_k=0,
+                            nn_order=_abi.ACO_NN_REFERENCE_QSORT,
+                            heuristic=_abi.ACO_HEURISTIC_LIBM,
+                            fallback=_abi.ACO_FALLBACK_REFERENCE, seed=1234)
+    threads = os.cpu_count() or 1
+    q = oracle.Port(p, d, threads=threads)
+    q.initialize()
+    for _ in range(args.warmup):
+        q.iterate()
+    tours = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        q.iterate()
+        tours += q.num_valid()
+    dt = time.perf_counter() - t0
+    v = tours / dt
+    return {"metric": "tours/s", "value": v, "unit": "tours/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD + " -- reference CPU algorithm: full-row roulette "
+                       "(no candidate lists), AS update (the reference's rank-based update is an "
+                       "empty stub)", "n": N_CITIES, "m": N_ANTS, "k": N_CITIES},
+            "cpu_baseline": {"value": v, "unit": "tours/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} iterations after {args.warmup} warm-up, "
+                                       f"C restatement of the reference CPU path, {threads} "
+                                       f"threads"},
+            "e2e": {"value": v, "unit": "tours/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import acogpu_gb300 as aco
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    x, y, d = workload_instance()
+    p = workload_params()
+    p.seed = 1234 + 7919 * rank  # independent replicas
+
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---------------- device-timed steps
+    col = aco.Colony(d, params=p, num_ants=N_ANTS)
+    col.set_stream(stream.cuda_stream)
+    col.initialize()
+    for _ in range(args.warmup):
+        col.constructSolution()
+    col.synchronize()
+    st0 = col.stats()
+    launches0 = col.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    stage = np.zeros(6)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()  # L2 flush, outside the timed events
+            ev[i][0].record(stream)
+            t = col.constructSolution(timers=True)
+            ev[i][1].record(stream)
+            stage += t
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_s = sum(step_ms) / 1e3
+    st1 = col.stats()
+    launches = col.launch_count() - launches0
+    tours = st1["tours_built"] - st0["tours_built"]
+    fallbacks = st1["fallbacks"] - st0["fallbacks"]
+    col.close()
+
+    # ---------------- end to end through the public API (host buffers)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    e = aco.Colony(d, params=p, num_ants=N_ANTS)
+    e.initialize()
+    d2h = 0
+    for _ in range(args.steps):
+        e.constructSolution()
+        e.getIterBestDist()
+        e.getGlobBestDist()
+        e.getNumValidAnts()
+        d2h += 3 * 96  # three state reads
+    tour = e.getTour()
+    d2h += 4 * N_CITIES
+    e_stats = e.stats()
+    torch.cuda.synchronize()
+    e_wall = time.perf_counter() - t0
+    e.close()
+    barrier()
+    e_tours = e_stats["tours_built"]
+
+    # max over ranks
+    vals = torch.tensor([dev_s, e_wall, wall], dtype=torch.float64, device=dev)
+    cnt = torch.tensor([tours, e_tours], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(vals, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(cnt, op=torch.distributed.ReduceOp.SUM)
+    dev_s, e_wall, wall = vals.tolist()
+    tours_all, e_tours_all = cnt.tolist()
+    if rank != 0:
+        return None
+
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    construct_s = stage[1] / 1e3
+    bytes_c = construct_bytes(N_CITIES, CAND_K, tours, fallbacks)
+    achieved = bytes_c / construct_s / 1e9
+    return {
+        "metric": "tours/s", "value": tours_all / dev_s, "unit": "tours/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+        "wall_ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": N_CITIES, "m": N_ANTS, "k": CAND_K, "w": RANK_W,
+                   "rho": RHO, "beta": BETA, "aging": True, "deposit": "deterministic",
+                   "iterations_per_step": 1,
+                   "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write, untimed)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "ant_steps_per_s": tours_all * (N_CITIES - 1) / dev_s,
+        "stage_ms_per_step": {"construct": stage[1] / args.steps,
+                              "epilogue": stage[2] / args.steps,
+                              "pheromone": stage[4] / args.steps},
+        "fallback_rate": fallbacks / max(1, tours * (N_CITIES - 1)),
+        "gpu_launches": int(launches) * world,
+        "roofline": {"bound": "hbm", "kernel": "k_construct", "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm else None,
+                     "algorithmic_bytes_per_launch": bytes_c / args.steps, "traffic": None},
+        "e2e": {"value": e_tours_all / e_wall, "unit": "tours/s",
+                "h2d_bytes_per_step": 4 * N_CITIES * N_CITIES / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps, "tour_head": tour[:24]},
+        "clocks": clk.summary(),
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world, local)
+    if out is not None:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -25,6 +25,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define ACO_API __attribute__((visibility("default")))
+#else
+#define ACO_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -92,6 +98,12 @@ enum aco_tau0_mode {
   ACO_TAU0_VALUE = 2      /* aco_params.tau0 */
 };
 
+enum aco_construct_mode {
+  ACO_CONSTRUCT_AUTO = 0,   /* staged when the candidate table fits in shared memory */
+  ACO_CONSTRUCT_GLOBAL = 1, /* candidate rows read from global memory (L2) */
+  ACO_CONSTRUCT_STAGED = 2  /* whole candidate table in shared memory; k <= 32 */
+};
+
 /* Stage timers filled by aco_colony_construct_solution, indexed like the
  * reference's StatsTimer enum (inc/Statistics.h:7-15). */
 enum aco_timer {
@@ -133,14 +145,15 @@ typedef struct aco_params {
                         (inc/broker/parallel.h:3, inc/Colony.h:142-149) */
   uint64_t seed;     /* seed of the injected uniform stream (acogpu_rng.h) */
   int32_t ants_per_block; /* construction warps per CTA; 0 = tuned default */
-  int32_t reserved[7];
+  int32_t construct_mode; /* enum aco_construct_mode */
+  int32_t reserved[6];
 } aco_params;
 
 /* Reference defaults (inc/default.h, src/Colony.cu:31-36): AS, m = 10,
  * alpha 1, beta 5, rho 0.1, full-row candidates, reference quicksort order,
  * libm heuristic, reference fallback, deterministic deposit, tau0 = 1e-6,
  * w = 5, noaging, aging parameters 30/50/10/10/40/100, seed 12345678. */
-void aco_params_default(aco_params *p);
+ACO_API void aco_params_default(aco_params *p);
 
 typedef struct aco_colony aco_colony;
 
@@ -153,76 +166,90 @@ typedef struct aco_colony aco_colony;
  * Replaces the constructors AntSystem::AntSystem (src/AntSystem.cu:160-182),
  * RankBasedAntSystem::RankBasedAntSystem (src/RankBasedAntSystem.cu:14-18)
  * and Colony::Colony (src/Colony.cu:25-137). */
-int aco_colony_create(const aco_params *params, const int32_t *dist, int32_t n,
+ACO_API int aco_colony_create(const aco_params *params, const int32_t *dist, int32_t n,
                       int32_t dist_on_device, aco_colony **out);
 
 /* Create a colony from float coordinates; the EUC_2D distance matrix
  * (reference: Utils::compute_distance, src/Utils.cu:162-182,212-218) is built
  * on the GPU. */
-int aco_colony_create_coords(const aco_params *params, const float *x,
+ACO_API int aco_colony_create_coords(const aco_params *params, const float *x,
                              const float *y, int32_t n, aco_colony **out);
 
 /* Colony::initialize (src/Colony.cu:185-214): initial pheromone, heuristic,
  * nn-list, aging state, best-so-far reset. */
-int aco_colony_initialize(aco_colony *c);
+ACO_API int aco_colony_initialize(aco_colony *c);
 
 /* Colony::constructSolution (src/Colony.cu:537-594): one iteration.  timers
  * (may be NULL) receives per-stage device times in ms, indexed by
  * enum aco_timer; passing timers makes the call synchronous. */
-int aco_colony_construct_solution(aco_colony *c, float *timers_ms);
+ACO_API int aco_colony_construct_solution(aco_colony *c, float *timers_ms);
 
 /* Run `iterations` iterations back to back from a captured CUDA graph, with
  * no host synchronisation in between.  Returns once they are enqueued. */
-int aco_colony_run(aco_colony *c, int32_t iterations);
+ACO_API int aco_colony_run(aco_colony *c, int32_t iterations);
 
 /* Wait for all enqueued work; reports device-side errors. */
-int aco_colony_synchronize(aco_colony *c);
+ACO_API int aco_colony_synchronize(aco_colony *c);
 
 /* Getters of the reference surface (inc/Colony.h:38-48,152). */
-int aco_colony_get_iter_best(aco_colony *c, int64_t *out);  /* getIterBestDist */
-int aco_colony_get_glob_best(aco_colony *c, int64_t *out);  /* getGlobBestDist */
-int aco_colony_get_num_valid_ants(aco_colony *c, int32_t *out); /* getNumValidAnts */
-int aco_colony_get_best_tour(aco_colony *c, int32_t *out_n);   /* getTour, 0-based */
-int aco_colony_get_iteration(aco_colony *c, int32_t *out);
-int aco_colony_get_reps(aco_colony *c, int32_t *out);        /* getReps (always 0) */
-int aco_colony_get_size(aco_colony *c, int32_t *n, int32_t *m, int32_t *k);
-int aco_colony_get_params(aco_colony *c, aco_params *out);
+ACO_API int aco_colony_get_iter_best(aco_colony *c, int64_t *out);  /* getIterBestDist */
+ACO_API int aco_colony_get_glob_best(aco_colony *c, int64_t *out);  /* getGlobBestDist */
+ACO_API int aco_colony_get_num_valid_ants(aco_colony *c, int32_t *out); /* getNumValidAnts */
+ACO_API int aco_colony_get_best_tour(aco_colony *c, int32_t *out_n);   /* getTour, 0-based */
+ACO_API int aco_colony_get_iteration(aco_colony *c, int32_t *out);
+ACO_API int aco_colony_get_reps(aco_colony *c, int32_t *out);        /* getReps (always 0) */
+ACO_API int aco_colony_get_size(aco_colony *c, int32_t *n, int32_t *m, int32_t *k);
+ACO_API int aco_colony_get_params(aco_colony *c, aco_params *out);
 /* Setters of the reference surface: setAlpha/setBeta/setRho/setOptimum
  * (inc/Colony.h:35-37,49), RankBasedAntSystem::setW, and the aging setters
  * (inc/Colony.h:128-139).  beta, w and tau0-relevant values take effect at
  * the next aco_colony_initialize. */
-int aco_colony_set_alpha(aco_colony *c, float v);
-int aco_colony_set_beta(aco_colony *c, float v);
-int aco_colony_set_rho(aco_colony *c, float v);
-int aco_colony_set_optimum(aco_colony *c, int64_t v);
-int aco_colony_set_rank_w(aco_colony *c, int32_t w);
-int aco_colony_set_aging_params(aco_colony *c, const int32_t six[6]);
+ACO_API int aco_colony_set_alpha(aco_colony *c, float v);
+ACO_API int aco_colony_set_beta(aco_colony *c, float v);
+ACO_API int aco_colony_set_rho(aco_colony *c, float v);
+ACO_API int aco_colony_set_optimum(aco_colony *c, int64_t v);
+ACO_API int aco_colony_set_rank_w(aco_colony *c, int32_t w);
+ACO_API int aco_colony_set_aging_params(aco_colony *c, const int32_t six[6]);
 /* antSystemName(): "Ant System" or "Rank-based Ant System". */
-const char *aco_colony_name(const aco_colony *c);
+ACO_API const char *aco_colony_name(const aco_colony *c);
 
 /* State export/import (host buffers), for checking and checkpointing. */
-int aco_colony_read_pheromone(aco_colony *c, float *out_nn);      /* n*n */
-int aco_colony_write_pheromone(aco_colony *c, const float *in_nn);
-int aco_colony_read_heuristic(aco_colony *c, float *out_nn);      /* n*n */
-int aco_colony_read_choice_info(aco_colony *c, float *out_nn);    /* n*n */
-int aco_colony_read_nn_list(aco_colony *c, int32_t *out_nk);      /* n*k */
-int aco_colony_read_distances(aco_colony *c, int32_t *out_nn);    /* n*n */
-int aco_colony_read_tours(aco_colony *c, int32_t *out_mn);        /* m*n */
-int aco_colony_read_tour_lengths(aco_colony *c, int64_t *out_m);
+ACO_API int aco_colony_read_pheromone(aco_colony *c, float *out_nn);      /* n*n */
+ACO_API int aco_colony_write_pheromone(aco_colony *c, const float *in_nn);
+ACO_API int aco_colony_read_heuristic(aco_colony *c, float *out_nn);      /* n*n */
+ACO_API int aco_colony_read_choice_info(aco_colony *c, float *out_nn);    /* n*n */
+ACO_API int aco_colony_read_nn_list(aco_colony *c, int32_t *out_nk);      /* n*k */
+ACO_API int aco_colony_read_distances(aco_colony *c, int32_t *out_nn);    /* n*n */
+ACO_API int aco_colony_read_tours(aco_colony *c, int32_t *out_mn);        /* m*n */
+ACO_API int aco_colony_read_tour_lengths(aco_colony *c, int64_t *out_m);
 /* age[m], performance[m], valid[m], pheromone row means[n],
  * misc[2] = {isconverged, globalperformance} */
-int aco_colony_read_aging(aco_colony *c, int32_t *age, int32_t *perf,
+ACO_API int aco_colony_read_aging(aco_colony *c, int32_t *age, int32_t *perf,
                           uint8_t *valid, float *mean, int32_t *misc);
 
+/* Counters kept on the device. */
+typedef struct aco_stats {
+  int64_t iteration;     /* iterations run since aco_colony_initialize */
+  int64_t tours_built;   /* tours constructed (valid ants) since initialize */
+  int64_t fallbacks;     /* construction steps resolved by the fallback rule */
+  int64_t greedy_length; /* C_nn of the tau0 rule (0 unless ACO_TAU0_DORIGO) */
+  int64_t iter_best;
+  int64_t glob_best;
+  int32_t num_valid;
+  float tau0;
+  int64_t reserved[4];
+} aco_stats;
+ACO_API int aco_colony_get_stats(aco_colony *c, aco_stats *out);
+
 /* Bind the colony to a CUDA stream (cudaStream_t passed as void*). */
-int aco_colony_set_stream(aco_colony *c, void *stream);
+ACO_API int aco_colony_set_stream(aco_colony *c, void *stream);
 /* Number of kernel launches this colony has issued (graph nodes count once
  * per replay). */
-int aco_colony_get_launch_count(aco_colony *c, int64_t *out);
+ACO_API int aco_colony_get_launch_count(aco_colony *c, int64_t *out);
 
-const char *aco_colony_last_error(const aco_colony *c);
-const char *aco_status_string(int status);
-void aco_colony_destroy(aco_colony *c);
+ACO_API const char *aco_colony_last_error(const aco_colony *c);
+ACO_API const char *aco_status_string(int status);
+ACO_API void aco_colony_destroy(aco_colony *c);
 
 #ifdef __cplusplus
 }
