@@ -132,7 +132,7 @@ int check_params(const aco_params *p, int n) {
   if (p->ants_per_block < 0 || p->ants_per_block > 16) return ACO_ERR_INVALID_ARGUMENT;
   if (p->construct_mode < ACO_CONSTRUCT_AUTO || p->construct_mode > ACO_CONSTRUCT_STAGED)
     return ACO_ERR_INVALID_ARGUMENT;
-  if (p->construct_mode == ACO_CONSTRUCT_STAGED && (K > 32 || n >= 32768))
+  if (p->construct_mode == ACO_CONSTRUCT_STAGED && (K > 32 || n > 2048))
     return ACO_ERR_UNSUPPORTED;
   return ACO_OK;
 }
@@ -231,7 +231,7 @@ cudaError_t launch_construction(aco_colony *c, const ColonyDev &d) {
 // memory, one CTA per SM) and the global-memory kernel.
 int plan_construction(aco_colony *c) {
   c->staged = false;
-  if (c->K > 32 || c->n >= 32768 || !c->nn16 || c->p.construct_mode == ACO_CONSTRUCT_GLOBAL)
+  if (c->K > 32 || c->n > 2048 || !c->nn16 || c->p.construct_mode == ACO_CONSTRUCT_GLOBAL)
     return ACO_OK;
   const int sms = c->num_sms > 0 ? c->num_sms : 1;
   int warps = (c->m + sms - 1) / sms;

@@ -12,10 +12,10 @@
 //    candidate order (ids + tau*eta, contiguous), masks visited cities and
 //    forms the prefix sums of the weights in candidate order.  The prefix is
 //    the sequential float sum of the reference (sum_prob += prob_ptr[i],
-//    src/Colony.cu:814; partial_sum += ..., :840): the 32 weights of a chunk
-//    are broadcast with __shfl_sync and added in lane order, so every
-//    partial sum is bit-identical to the CPU's (adding the zero weight of a
-//    visited city changes nothing, as in the reference);
+//    src/Colony.cu:814; partial_sum += ..., :840): the non-zero weights of a
+//    chunk are compacted by ballot and added in lane order, so every partial
+//    sum is bit-identical to the CPU's (the zero weight of a visited city
+//    changes no sum);
 //  * the crossing `first i with partial_sum > u * sum` is a ballot; rows
 //    longer than 32 candidates keep the prefix at each chunk end in shared
 //    memory and redo only the chunk that holds the crossing;
@@ -45,16 +45,39 @@ __device__ __forceinline__ bool visited(const uint32_t *tabu, int city) {
   return (tabu[city >> 5] >> (city & 31)) & 1u;
 }
 
-// s + w[0] + w[1] + ... + w[31] in lane order (each addition rounded);
-// p receives the prefix that includes this lane's weight.
-__device__ __forceinline__ float fold32(float s, float w, int lane, float &p) {
-  p = s;
-#pragma unroll
-  for (int b = 0; b < 32; b++) {
-    const float v = __shfl_sync(kFull, w, b);
-    s = __fadd_rn(s, v);
-    p = (lane == b) ? s : p;
+// Ordered fold of one chunk of 32 candidates.  The reference adds every
+// weight of the row in order, zeros included (src/Colony.cu:801-816); adding
+// +0 leaves a non-negative float sum unchanged, so only the non-zero weights
+// need to be added, still in lane order.  They are compacted through a
+// 32-float shared buffer (ballot + popc rank), then folded with broadcast
+// reads; `mine` receives the prefix that ends at this lane's weight (only
+// meaningful for lanes with a non-zero weight).
+__device__ __forceinline__ float fold_nonzero(float s, float w, int lane, float *wbuf,
+                                              float &mine) {
+  const unsigned nz = __ballot_sync(kFull, w != 0.0f);
+  const int cnt = __popc(nz);
+  const int rank = __popc(nz & ((1u << lane) - 1u));
+  if (w != 0.0f) wbuf[rank] = w;
+  __syncwarp();
+  mine = s;
+  int i = 0;
+#pragma unroll 1
+  for (; i + 4 <= cnt; i += 4) {
+    const float a0 = wbuf[i], a1 = wbuf[i + 1], a2 = wbuf[i + 2], a3 = wbuf[i + 3];
+    s = __fadd_rn(s, a0);
+    mine = (rank == i) ? s : mine;
+    s = __fadd_rn(s, a1);
+    mine = (rank == i + 1) ? s : mine;
+    s = __fadd_rn(s, a2);
+    mine = (rank == i + 2) ? s : mine;
+    s = __fadd_rn(s, a3);
+    mine = (rank == i + 3) ? s : mine;
   }
+  for (; i < cnt; i++) {
+    s = __fadd_rn(s, wbuf[i]);
+    mine = (rank == i) ? s : mine;
+  }
+  __syncwarp();
   return s;
 }
 
@@ -114,20 +137,36 @@ __device__ int fallback_city(const ColonyDev &c, int cur, const uint32_t *tabu, 
     }
     return -1;
   }
-  // Largest choice value among unvisited cities, lowest index on ties.
+  // Largest choice value among unvisited cities, lowest index on ties.  Each
+  // lane scans groups of 4 consecutive cities with float4 loads (rows are
+  // 128-byte aligned); the loads of a lane are independent of each other.
   float bw = -1.0f;
   int bj = -1;
   const float *crow = c.choice + (size_t)cur * c.ld;
   const float *trow = c.tau + (size_t)cur * c.ld;
   const float *erow = c.eta + (size_t)cur * c.ld;
-  for (int j = lane; j < c.n; j += 32) {
-    if (visited(tabu, j)) continue;
-    const float w = a.blend ? blend_fitness(trow[j], erow[j], a.meanc, a.ratio, c.use_alpha,
-                                            c.alpha)
-                            : crow[j];
-    if (w > bw) {
-      bw = w;
-      bj = j;
+#pragma unroll 2
+  for (int j4 = lane * 4; j4 < c.n; j4 += 128) {
+    const uint32_t bits = (tabu[j4 >> 5] >> (j4 & 31)) & 0xfu;
+    if (bits == 0xfu) continue;
+    float v[4];
+    if (!a.blend) {
+      const float4 q = *reinterpret_cast<const float4 *>(crow + j4);
+      v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
+      const float4 t = *reinterpret_cast<const float4 *>(trow + j4);
+      const float4 e = *reinterpret_cast<const float4 *>(erow + j4);
+      v[0] = blend_fitness(t.x, e.x, a.meanc, a.ratio, c.use_alpha, c.alpha);
+      v[1] = blend_fitness(t.y, e.y, a.meanc, a.ratio, c.use_alpha, c.alpha);
+      v[2] = blend_fitness(t.z, e.z, a.meanc, a.ratio, c.use_alpha, c.alpha);
+      v[3] = blend_fitness(t.w, e.w, a.meanc, a.ratio, c.use_alpha, c.alpha);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (!((bits >> q) & 1u) && j4 + q < c.n && v[q] > bw) {
+        bw = v[q];
+        bj = j4 + q;
+      }
     }
   }
   for (int o = 16; o; o >>= 1) {
@@ -143,7 +182,7 @@ __device__ int fallback_city(const ColonyDev &c, int cur, const uint32_t *tabu, 
 
 template <bool MULTI, bool AGING, bool STAGED>
 __device__ void construct_ant(const ColonyDev &c, int k, uint32_t iter, uint32_t *tabu,
-                              float *cend, const int16_t *sids, const float *scw,
+                              float *cend, float *wbuf, const int16_t *sids, const float *scw,
                               const float *smean, int nchunks, int lane) {
   const int n = c.n;
   const int words = (n + 31) >> 5;
@@ -171,7 +210,8 @@ __device__ void construct_ant(const ColonyDev &c, int k, uint32_t iter, uint32_t
   __syncwarp();
 
   // initTour placement (src/Colony.cu:518-520)
-  const float u0 = aco_uniform(c.seed, iter, (uint32_t)k, 0u);
+  const uint32_t akey = aco_ant_key(c.seed, iter, (uint32_t)k);
+  const float u0 = aco_uniform_key(akey, 0u);
   int start = __float2int_rz(__fmul_rn(u0, __int2float_rn(n)));
   if (start >= n) {  // impossible for u0 < 1; recorded, clamped
     if (lane == 0) atomicOr(&c.st->error, kErrCheck);
@@ -186,7 +226,7 @@ __device__ void construct_ant(const ColonyDev &c, int k, uint32_t iter, uint32_t
   int cur = start;
   int64_t fallbacks = 0;
   for (int x = 1; x < n; x++) {
-    const float u = aco_uniform(c.seed, iter, (uint32_t)k, (uint32_t)x);
+    const float u = aco_uniform_key(akey, (uint32_t)x);
     if (AGING && a.blend) a.meanc = STAGED ? smean[cur] : c.mean[cur];
     int next = -1;
     if (!MULTI) {
@@ -194,10 +234,10 @@ __device__ void construct_ant(const ColonyDev &c, int k, uint32_t iter, uint32_t
       float w;
       candidate<STAGED>(c, cur, lane, tabu, sids, scw, a, id, w);
       float p;
-      const float S = fold32(0.0f, w, lane, p);
+      const float S = fold_nonzero(0.0f, w, lane, wbuf, p);
       if (!(S <= 0.0f)) {
         const float rnd = __fmul_rn(u, S);
-        const unsigned hit = __ballot_sync(kFull, lane < c.K && !(p <= rnd));
+        const unsigned hit = __ballot_sync(kFull, w != 0.0f && !(p <= rnd));
         if (hit) next = __shfl_sync(kFull, id, __ffs(hit) - 1);
       }
     } else {
@@ -208,7 +248,7 @@ __device__ void construct_ant(const ColonyDev &c, int k, uint32_t iter, uint32_t
         candidate<false>(c, cur, ch * 32 + lane, tabu, sids, scw, a, id, w);
         if (__ballot_sync(kFull, w != 0.0f)) {
           float p;
-          s = fold32(s, w, lane, p);
+          s = fold_nonzero(s, w, lane, wbuf, p);
         }
         if (lane == 0) cend[ch] = s;
       }
@@ -232,8 +272,8 @@ __device__ void construct_ant(const ColonyDev &c, int k, uint32_t iter, uint32_t
           float w;
           candidate<false>(c, cur, r, tabu, sids, scw, a, id, w);
           float p;
-          fold32(s0, w, lane, p);
-          const unsigned hit = __ballot_sync(kFull, r < c.K && !(p <= rnd));
+          fold_nonzero(s0, w, lane, wbuf, p);
+          const unsigned hit = __ballot_sync(kFull, w != 0.0f && !(p <= rnd));
           if (hit) next = __shfl_sync(kFull, id, __ffs(hit) - 1);
         }
       }
@@ -266,7 +306,238 @@ __device__ void construct_ant(const ColonyDev &c, int k, uint32_t iter, uint32_t
   for (int i = lane; i < n; i += 32) {
     const int a0 = trow[i];
     const int b0 = trow[i + 1 == n ? 0 : i + 1];
-    len += c.dist[(size_t)a0 * c.ld + b0];
+    if ((unsigned)a0 < (unsigned)n && (unsigned)b0 < (unsigned)n)
+      len += c.dist[(size_t)a0 * c.ld + b0];
+    else
+      atomicOr(&c.st->error, kErrCheck);
+  }
+  for (int o = 16; o; o >>= 1) len += __shfl_xor_sync(kFull, len, o);
+  if (lane == 0) {
+    c.newlen[k] = len;
+    if (fallbacks)
+      atomicAdd(reinterpret_cast<unsigned long long *>(&c.st->fallbacks),
+                (unsigned long long)fallbacks);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Staged construction step, specialised for the short critical path of one
+// ant: candidate rows in shared memory, the tabu bitmask in registers (lane
+// l owns the 32-city words l, l+32, ...; a lookup is one __shfl_sync and the
+// owner lane sets the bit), the non-zero weights compacted into a
+// zero-padded 32-float buffer and folded in lane order from broadcast
+// 16-byte reads.
+template <int TW>
+__device__ __forceinline__ bool reg_visited(const uint32_t (&tw)[TW], int city) {
+  const int word = city >> 5;
+  uint32_t v = __shfl_sync(kFull, tw[0], word & 31);
+  if (TW > 1) {
+    const uint32_t v1 = __shfl_sync(kFull, tw[TW > 1 ? 1 : 0], word & 31);
+    v = (word >> 5) ? v1 : v;
+  }
+  return (v >> (city & 31)) & 1u;
+}
+
+template <int TW>
+__device__ __forceinline__ void reg_mark(uint32_t (&tw)[TW], int city, int lane) {
+  const int word = city >> 5;
+  if (lane == (word & 31)) {
+    if (TW == 1 || (word >> 5) == 0)
+      tw[0] |= 1u << (city & 31);
+    else
+      tw[TW > 1 ? 1 : 0] |= 1u << (city & 31);
+  }
+}
+
+// Largest choice value among unvisited cities (register tabu version).
+template <int TW>
+__device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&tw)[TW],
+                                 const AntCtx &a, int lane) {
+  float bw = -1.0f;
+  int bj = -1;
+  const float *crow = c.choice + (size_t)cur * c.ld;
+  const float *trow = c.tau + (size_t)cur * c.ld;
+  const float *erow = c.eta + (size_t)cur * c.ld;
+  for (int base = 0; base < c.n; base += 128) {
+    const int j4 = base + lane * 4;
+    const int word = j4 >> 5;  // warp-uniform source per lane group
+    uint32_t v = __shfl_sync(kFull, tw[0], word & 31);
+    if (TW > 1) {
+      const uint32_t v1 = __shfl_sync(kFull, tw[TW > 1 ? 1 : 0], word & 31);
+      v = (word >> 5) ? v1 : v;
+    }
+    if (j4 >= c.n) continue;
+    const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
+    if (bits == 0xfu) continue;
+    float q[4];
+    if (!a.blend) {
+      const float4 t = *reinterpret_cast<const float4 *>(crow + j4);
+      q[0] = t.x; q[1] = t.y; q[2] = t.z; q[3] = t.w;
+    } else {
+      const float4 t = *reinterpret_cast<const float4 *>(trow + j4);
+      const float4 e = *reinterpret_cast<const float4 *>(erow + j4);
+      q[0] = blend_fitness(t.x, e.x, a.meanc, a.ratio, c.use_alpha, c.alpha);
+      q[1] = blend_fitness(t.y, e.y, a.meanc, a.ratio, c.use_alpha, c.alpha);
+      q[2] = blend_fitness(t.z, e.z, a.meanc, a.ratio, c.use_alpha, c.alpha);
+      q[3] = blend_fitness(t.w, e.w, a.meanc, a.ratio, c.use_alpha, c.alpha);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      if (!((bits >> r) & 1u) && j4 + r < c.n && q[r] > bw) {
+        bw = q[r];
+        bj = j4 + r;
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    const float ow = __shfl_xor_sync(kFull, bw, o);
+    const int oj = __shfl_xor_sync(kFull, bj, o);
+    if (oj >= 0 && (bj < 0 || ow > bw || (ow == bw && oj < bj))) {
+      bw = ow;
+      bj = oj;
+    }
+  }
+  return bj;
+}
+
+// The step loop of one ant; BLEND (the aging fitness blend, fixed for the
+// ant's whole tour) is a template parameter so the loop carries no per-step
+// test of it.  Rows of the staged table are padded to 32 entries with id -1
+// and weight 0, so every lane loads unconditionally.
+template <int TW, bool BLEND>
+__device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t akey, int start,
+                                            uint32_t (&tw)[TW], float *wbuf, const int16_t *sids,
+                                            const float *scw, const float *smean, AntCtx a,
+                                            int lane, int64_t &fallbacks) {
+  const int n = c.n;
+  int32_t *trow = c.tours + (size_t)k * c.ld;
+  const unsigned lt = (1u << lane) - 1u;
+  const float4 *wbuf4 = reinterpret_cast<const float4 *>(wbuf);
+  int cur = start;
+  for (int x = 1; x < n; x++) {
+    const float u = aco_uniform_key(akey, (uint32_t)x);
+    const int id = sids[cur * 32 + lane];
+    float w;
+    if (!BLEND) {
+      w = scw[cur * 32 + lane];
+    } else {
+      a.meanc = smean[cur];  // every lane: the fallback scan uses it too
+      const size_t off = (size_t)cur * c.ldk + lane;
+      w = lane < c.K ? blend_fitness(c.tau_nn[off], __ldg(c.eta_nn + off), a.meanc, a.ratio,
+                                     c.use_alpha, c.alpha)
+                     : 0.0f;
+    }
+    // reg_visited shuffles with the full mask: every lane must call it.
+    const bool vis = reg_visited(tw, id < 0 ? 0 : id);
+    const bool unvisited = id >= 0 && !vis;
+    if (!unvisited) w = 0.0f;
+    const unsigned nz = __ballot_sync(kFull, w != 0.0f);
+    const int cnt = __popc(nz);
+    int next = -1;
+    if (cnt > 0) {
+      const bool mine_nz = w != 0.0f;
+      const int rank = __popc(nz & lt);
+      wbuf[mine_nz ? rank : cnt + __popc(~nz & lt)] = w;
+      __syncwarp();
+      float s = 0.0f, mine = 0.0f;
+#pragma unroll
+      for (int g = 0; g < 4; g++) {
+        if (g * 8 < cnt) {
+          const float4 p0 = wbuf4[2 * g], p1 = wbuf4[2 * g + 1];
+          const float v[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+#pragma unroll
+          for (int e = 0; e < 8; e++) {
+            s = __fadd_rn(s, v[e]);
+            mine = (rank == g * 8 + e) ? s : mine;
+          }
+        }
+      }
+      __syncwarp();
+      const float rnd = __fmul_rn(u, s);
+      const unsigned hit = __ballot_sync(kFull, mine_nz && !(mine <= rnd));
+      if (hit) next = __shfl_sync(kFull, id, __ffs(hit) - 1);
+      if (next >= n) {  // a candidate id outside the instance: recorded, not used
+        if (lane == 0) atomicOr(&c.st->error, kErrCheck);
+        return cur;
+      }
+    }
+    if (next < 0) {
+      if (c.fallback == ACO_FALLBACK_BEST) {
+        next = fallback_best_reg(c, cur, tw, a, lane);
+      } else {  // select_local_best on a full row of at most 32 cities (k == n)
+        const unsigned um = __ballot_sync(kFull, unvisited);
+        next = um ? __shfl_sync(kFull, id, 31 - __clz(um)) : -1;
+      }
+      fallbacks++;
+      if (next < 0 || next >= n) {  // no unvisited city (or a rule that needs a full row)
+        if (lane == 0) atomicOr(&c.st->error, kErrCheck);
+        return cur;
+      }
+    }
+    reg_mark(tw, next, lane);
+    if (lane == 0) trow[x] = next;
+    if (lane == 1) c.succT[(size_t)cur * c.ldm + k] = next;
+    if (lane == 2) c.predT[(size_t)next * c.ldm + k] = cur;
+    cur = next;
+  }
+  return cur;
+}
+
+template <bool AGING, int TW>
+__device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
+                                     const int16_t *sids, const float *scw, const float *smean,
+                                     int lane) {
+  const int n = c.n;
+  int32_t *trow = c.tours + (size_t)k * c.ld;
+  AntCtx a;
+  a.blend = false;
+  a.ratio = 0.0f;
+  a.meanc = 0.0f;
+  if (AGING) {
+    int age = 0;
+    if (lane == 0) {
+      age = c.age[k] + 1;
+      c.age[k] = age;
+    }
+    age = __shfl_sync(kFull, age, 0);
+    if (!c.valid[k]) {  // invalid ants keep a cleared tour (src/Colony.cu:507-510)
+      for (int i = lane; i < n; i += 32) trow[i] = 0;
+      return;
+    }
+    a.blend = age < c.min_ret && c.st->isconverged;
+    if (a.blend) a.ratio = __fdiv_rn(__int2float_rn(age), __int2float_rn(c.min_ret));
+  }
+  uint32_t tw[TW];
+#pragma unroll
+  for (int t = 0; t < TW; t++) tw[t] = 0u;
+
+  // initTour placement (src/Colony.cu:518-520)
+  const uint32_t akey = aco_ant_key(c.seed, iter, (uint32_t)k);
+  int start = __float2int_rz(__fmul_rn(aco_uniform_key(akey, 0u), __int2float_rn(n)));
+  if (start >= n) {  // impossible for u < 1; recorded, clamped
+    if (lane == 0) atomicOr(&c.st->error, kErrCheck);
+    start = n - 1;
+  }
+  reg_mark(tw, start, lane);
+  if (lane == 0) trow[0] = start;
+
+  int64_t fallbacks = 0;
+  const int last = (AGING && a.blend)
+                       ? staged_steps<TW, true>(c, k, akey, start, tw, wbuf, sids, scw, smean, a,
+                                                lane, fallbacks)
+                       : staged_steps<TW, false>(c, k, akey, start, tw, wbuf, sids, scw, smean, a,
+                                                 lane, fallbacks);
+  if (lane == 1) c.succT[(size_t)last * c.ldm + k] = start;
+  if (lane == 2) c.predT[(size_t)start * c.ldm + k] = last;
+  __syncwarp();
+  int64_t len = 0;
+  for (int i = lane; i < n; i += 32) {
+    const int a0 = trow[i];
+    const int b0 = trow[i + 1 == n ? 0 : i + 1];
+    if ((unsigned)a0 < (unsigned)n && (unsigned)b0 < (unsigned)n)
+      len += c.dist[(size_t)a0 * c.ld + b0];
+    else
+      atomicOr(&c.st->error, kErrCheck);
   }
   for (int o = 16; o; o >>= 1) len += __shfl_xor_sync(kFull, len, o);
   if (lane == 0) {
@@ -284,30 +555,30 @@ __global__ void __launch_bounds__(512) k_construct(ColonyDev c, int nchunks) {
   const int k = blockIdx.x * (blockDim.x >> 5) + warp;
   if (k >= c.m) return;
   const int words = (c.n + 31) >> 5;
-  uint32_t *tabu = smem_construct + (size_t)warp * (words + (MULTI ? nchunks : 0));
-  float *cend = reinterpret_cast<float *>(tabu + words);
-  construct_ant<MULTI, AGING, false>(c, k, c.st->iteration, tabu, cend, nullptr, nullptr,
+  uint32_t *tabu = smem_construct + (size_t)warp * (words + 32 + (MULTI ? nchunks : 0));
+  float *wbuf = reinterpret_cast<float *>(tabu + words);
+  float *cend = wbuf + 32;
+  construct_ant<MULTI, AGING, false>(c, k, c.st->iteration, tabu, cend, wbuf, nullptr, nullptr,
                                      nullptr, nchunks, lane);
 }
 
 // Shared-memory layout of the staged kernel:
-//   [choice n*32 f32][ids n*32 int16][mean ld f32, aging][tabu words per warp][mbarrier]
+//   [choice n*32 f32][ids n*32 int16][mean ld f32, aging][per warp: 32 f32][mbarrier]
 __host__ __device__ inline size_t staged_table_bytes(int n, int ld, bool aging) {
   return (size_t)n * 32 * 4 + (size_t)n * 32 * 2 + (aging ? (size_t)ld * 4 : 0);
 }
 
-template <bool AGING>
+template <bool AGING, int TW>
 __global__ void __launch_bounds__(1024) k_construct_staged(ColonyDev c, const int16_t *nn16) {
   extern __shared__ __align__(128) unsigned char smem_staged[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
-  const int n = c.n, words = (n + 31) >> 5;
+  const int n = c.n;
   float *scw = reinterpret_cast<float *>(smem_staged);
   int16_t *sids = reinterpret_cast<int16_t *>(smem_staged + (size_t)n * 128);
   float *smean = reinterpret_cast<float *>(smem_staged + (size_t)n * 192);
-  const size_t table = staged_table_bytes(n, c.ld, AGING);
-  uint32_t *tabu = reinterpret_cast<uint32_t *>(smem_staged + table) + (size_t)warp * words;
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_staged + table + (size_t)warps * words * 4 +
-                                               ((8 - ((table + (size_t)warps * words * 4) & 7)) & 7));
+  const size_t table = staged_table_bytes(n, c.ld, AGING);  // a multiple of 64 bytes
+  float *wbuf = reinterpret_cast<float *>(smem_staged + table) + (size_t)warp * 32;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_staged + table + (size_t)warps * 128);
   __shared__ int flag;
 
   if (threadIdx.x == 0) {
@@ -333,19 +604,18 @@ __global__ void __launch_bounds__(1024) k_construct_staged(ColonyDev c, const in
   if (!flag) return;
   const uint32_t iter = c.st->iteration;
   for (int k = blockIdx.x * warps + warp; k < c.m; k += gridDim.x * warps)
-    construct_ant<false, AGING, true>(c, k, iter, tabu, nullptr, sids, scw, smean, 1, lane);
+    construct_ant_staged<AGING, TW>(c, k, iter, wbuf, sids, scw, smean, lane);
 }
 
 size_t construct_smem_bytes(int n, int K, int ants_per_block) {
   const int words = (n + 31) / 32;
   const int nchunks = (K + 31) / 32;
-  const int per_warp = words + (K > 32 ? nchunks : 0);
+  const int per_warp = words + 32 + (K > 32 ? nchunks : 0);
   return (size_t)ants_per_block * per_warp * 4;
 }
 
 size_t construct_staged_smem_bytes(int n, int ld, bool aging, int warps) {
-  const size_t words = (size_t)(n + 31) / 32;
-  return staged_table_bytes(n, ld, aging) + (size_t)warps * words * 4 + 16;
+  return staged_table_bytes(n, ld, aging) + (size_t)warps * 128 + 16;
 }
 
 cudaError_t configure_construct(size_t smem) {
@@ -363,11 +633,13 @@ cudaError_t configure_construct(size_t smem) {
 
 cudaError_t configure_construct_staged(size_t smem) {
   const int v = (int)smem;
-  cudaError_t e = cudaFuncSetAttribute(k_construct_staged<true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_construct_staged<false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  cudaError_t e = cudaSuccess;
+  const void *fns[4] = {(const void *)k_construct_staged<true, 1>,
+                        (const void *)k_construct_staged<false, 1>,
+                        (const void *)k_construct_staged<true, 2>,
+                        (const void *)k_construct_staged<false, 2>};
+  for (int i = 0; i < 4 && e == cudaSuccess; i++)
+    e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, v);
   return e;
 }
 
@@ -390,11 +662,20 @@ cudaError_t launch_construct(const ColonyDev &c, int apb, cudaStream_t s) {
 
 cudaError_t launch_construct_staged(const ColonyDev &c, const int16_t *nn16, int grid, int warps,
                                     cudaStream_t s) {
+  if (c.n > 2048) return cudaErrorInvalidValue;
   const size_t smem = construct_staged_smem_bytes(c.n, c.ld, c.aging, warps);
-  if (c.aging)
-    k_construct_staged<true><<<grid, warps * 32, smem, s>>>(c, nn16);
-  else
-    k_construct_staged<false><<<grid, warps * 32, smem, s>>>(c, nn16);
+  const bool two = c.n > 1024;
+  if (c.aging) {
+    if (two)
+      k_construct_staged<true, 2><<<grid, warps * 32, smem, s>>>(c, nn16);
+    else
+      k_construct_staged<true, 1><<<grid, warps * 32, smem, s>>>(c, nn16);
+  } else {
+    if (two)
+      k_construct_staged<false, 2><<<grid, warps * 32, smem, s>>>(c, nn16);
+    else
+      k_construct_staged<false, 1><<<grid, warps * 32, smem, s>>>(c, nn16);
+  }
   return cudaGetLastError();
 }
 

@@ -1,34 +1,44 @@
 """numpy restatement of the injected uniform stream of include/acogpu_rng.h
-(for inspection and tests; the kernels use the header itself)."""
+(for inspection and tests; the kernels and the oracle use the header)."""
 import numpy as np
 
-_M1 = np.uint64(0xBF58476D1CE4E5B9)
-_M2 = np.uint64(0x94D049BB133111EB)
+_U32 = np.uint32
 
 
-def mix64(z):
-    z = np.asarray(z, dtype=np.uint64)
+def hash32(x):
+    """lowbias32 (Wellons 2018) on uint32 arrays."""
+    x = np.asarray(x, dtype=np.uint32)
     with np.errstate(over="ignore"):
-        z = (z ^ (z >> np.uint64(30))) * _M1
-        z = (z ^ (z >> np.uint64(27))) * _M2
-    return z ^ (z >> np.uint64(31))
+        x = x ^ (x >> _U32(16))
+        x = x * _U32(0x7FEB352D)
+        x = x ^ (x >> _U32(15))
+        x = x * _U32(0x846CA68B)
+        x = x ^ (x >> _U32(16))
+    return x
 
 
-def key(iteration, ant, step):
-    it = np.uint64(iteration & 0x3FFFFF)
-    a = np.asarray(ant, dtype=np.uint64) & np.uint64(0x1FFFFF)
-    s = np.asarray(step, dtype=np.uint64) & np.uint64(0x1FFFFF)
-    return (it << np.uint64(42)) | (a << np.uint64(21)) | s
+def ant_key(seed, iteration, ant):
+    lo = _U32(seed & 0xFFFFFFFF)
+    hi = _U32((seed >> 32) & 0xFFFFFFFF)
+    with np.errstate(over="ignore"):
+        h = hash32(lo ^ hash32(hi + _U32(0x9E3779B9)))
+        h = hash32(h ^ (_U32(iteration & 0xFFFFFFFF) * _U32(0x9E3779B9) + _U32(0x632BE5AB)))
+        a = np.asarray(ant, dtype=np.uint32)
+        return hash32(h ^ (a * _U32(0x85EBCA6B) + _U32(0xC2B2AE35)))
 
 
-def uniform(seed, iteration, ant, step):
-    h = mix64(mix64(np.uint64(seed)) ^ key(iteration, ant, step))
-    top = (h >> np.uint64(40)).astype(np.uint32)
+def uniform_key(key, step):
+    with np.errstate(over="ignore"):
+        top = hash32(np.asarray(key, dtype=np.uint32) +
+                     np.asarray(step, dtype=np.uint32) * _U32(0x9E3779B9)) >> _U32(8)
     u = top.astype(np.float32) * np.float32(2.0 ** -24)
     return np.where(top == 0, np.float32(2.0 ** -25), u)
 
 
+def uniform(seed, iteration, ant, step):
+    return uniform_key(ant_key(seed, iteration, ant), step)
+
+
 def uniform_grid(seed, iteration, ants, steps):
-    a = np.asarray(ants)[:, None]
-    s = np.asarray(steps)[None, :]
-    return uniform(seed, iteration, a, s)
+    k = ant_key(seed, iteration, np.asarray(ants))[:, None]
+    return uniform_key(k, np.asarray(steps)[None, :])

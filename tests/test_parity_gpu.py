@@ -87,6 +87,9 @@ FAST_MODE = dict(nn_order=_abi.ACO_NN_STABLE, heuristic=_abi.ACO_HEURISTIC_DEVIC
 
 
 @pytest.mark.parametrize("case", [
+    dict(n=24, m=16, beta=2.0, rho=0.5, iters=10, **REFERENCE_MODE),
+    dict(n=31, m=20, beta=2.0, rho=0.3, iters=20, aging=1, six=(3, 5, 10, 2, 10, 100),
+         **REFERENCE_MODE),
     dict(n=60, m=40, beta=2.0, rho=0.5, iters=8, **REFERENCE_MODE),
     dict(n=97, m=33, beta=5.0, rho=0.1, iters=6, kind="clustered", **REFERENCE_MODE),
     dict(n=50, m=30, beta=2.0, rho=0.3, iters=30, aging=1, six=(3, 5, 10, 2, 15, 100),
