@@ -313,6 +313,14 @@ int aco_colony_create(const aco_params *params, const int32_t *dist, int32_t n,
   aco_colony *c = nullptr;
   int s = create_common(params, n, out, &c);
   if (s) return s;
+  if (dist_on_device < 0) {  // locate the pointer (the reference passes either kind)
+    cudaPointerAttributes attr;
+    dist_on_device = (cudaPointerGetAttributes(&attr, dist) == cudaSuccess &&
+                      (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged))
+                         ? 1
+                         : 0;
+    cudaGetLastError();  // clear a possible "invalid value" from a plain host pointer
+  }
   const cudaMemcpyKind kind = dist_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   cudaError_t e = cudaMemcpy2DAsync(c->dist, (size_t)c->ld * 4, dist, (size_t)n * 4,
                                     (size_t)n * 4, n, kind, c->stream);

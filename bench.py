@@ -116,6 +116,18 @@ def peaks():
         return {}
 
 
+def profiled_traffic(name="construct_staged_rbas_aging_n1000.md"):
+    """DRAM bytes per launch of the construction kernel, from the committed
+    ncu summary (dram__bytes_read.sum + dram__bytes_write.sum of one capture)."""
+    try:
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
 def construct_bytes(n, k, tours, fallbacks):
     """Algorithmic bytes of the construction kernel: per ant-step the k
     candidate ids and k choice weights (8k), the tour write and the distance
@@ -244,7 +256,7 @@ def run_ours(args, rank, world, local):
         e.getIterBestDist()
         e.getGlobBestDist()
         e.getNumValidAnts()
-        d2h += 3 * 96  # three state reads
+        d2h += 3 * 96  # three state reads (the device state block, padded)
     tour = e.getTour()
     d2h += 4 * N_CITIES
     e_stats = e.stats()
@@ -289,7 +301,9 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "hbm", "kernel": "k_construct", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm else None,
-                     "algorithmic_bytes_per_launch": bytes_c / args.steps, "traffic": None},
+                     "algorithmic_bytes_per_launch": bytes_c / args.steps,
+                     "traffic": profiled_traffic(),
+                     "traffic_source": "profiles/construct_staged_rbas_aging_n1000.md (ncu)"},
         "e2e": {"value": e_tours_all / e_wall, "unit": "tours/s",
                 "h2d_bytes_per_step": 4 * N_CITIES * N_CITIES / args.steps,
                 "d2h_bytes_per_step": d2h / args.steps, "tour_head": tour[:24]},

@@ -162,7 +162,7 @@ typedef struct aco_colony aco_colony;
  *         diagonal (the reference's distance vector, src/Setup.cpp:54-70).
  *   dist_on_device: 0 if dist is host memory, 1 if it is device memory on the
  *         current device (the reference GPU build passes a device pointer,
- *         src/Setup.cpp:60-66).
+ *         src/Setup.cpp:60-66), -1 to let the library find out.
  * Replaces the constructors AntSystem::AntSystem (src/AntSystem.cu:160-182),
  * RankBasedAntSystem::RankBasedAntSystem (src/RankBasedAntSystem.cu:14-18)
  * and Colony::Colony (src/Colony.cu:25-137). */
