@@ -74,6 +74,16 @@ class AcoStats(ctypes.Structure):
     ]
 
 
+class AcoTuning(ctypes.Structure):
+    _fields_ = [
+        ("ants_per_block", ctypes.c_int32),
+        ("row_threads", ctypes.c_int32),
+        ("construct_ms", ctypes.c_float),
+        ("rows_ms", ctypes.c_float),
+        ("reserved", ctypes.c_int32 * 4),
+    ]
+
+
 def default_params(**overrides):
     """Reference defaults (inc/default.h, src/Colony.cu:31-36); keyword
     arguments override fields by name."""

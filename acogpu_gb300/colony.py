@@ -83,6 +83,22 @@ def lib():
     L.aco_status_string.restype = ctypes.c_char_p
     L.aco_colony_destroy.argtypes = [_vp]
     L.aco_colony_destroy.restype = None
+    L.aco_batch_create.argtypes = [ctypes.POINTER(AcoParams), ctypes.c_int32, _i32p, _f32p,
+                                   ctypes.POINTER(_vp)]
+    for name in ("aco_batch_initialize", "aco_batch_synchronize"):
+        getattr(L, name).argtypes = [_vp]
+    L.aco_batch_run.argtypes = [_vp, ctypes.c_int32]
+    L.aco_batch_autotune.argtypes = [_vp, ctypes.POINTER(_abi.AcoTuning)]
+    L.aco_batch_set_tuning.argtypes = [_vp, ctypes.c_int32, ctypes.c_int32]
+    L.aco_batch_get_size.argtypes = [_vp, _i32p]
+    L.aco_batch_get_colony.argtypes = [_vp, ctypes.c_int32, ctypes.POINTER(_vp)]
+    for name in ("aco_batch_get_glob_best", "aco_batch_get_tours_built",
+                 "aco_batch_get_launch_count"):
+        getattr(L, name).argtypes = [_vp, _i64p]
+    L.aco_batch_last_error.argtypes = [_vp]
+    L.aco_batch_last_error.restype = ctypes.c_char_p
+    L.aco_batch_destroy.argtypes = [_vp]
+    L.aco_batch_destroy.restype = None
     _lib_handle = L
     return L
 
@@ -359,3 +375,106 @@ class RankBasedAntSystem(Colony):
 
     def getW(self):
         return self._params().rank_w
+
+
+class _BorrowedColony(Colony):
+    """Read-only view of one instance of a Batch (no ownership)."""
+
+    def __init__(self, L, handle, params):
+        self._L = L
+        self._h = handle
+        n, m, k = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        L.aco_colony_get_size(handle, ctypes.byref(n), ctypes.byref(m), ctypes.byref(k))
+        self.n, self.m, self.k = n.value, m.value, k.value
+        self.params = params
+
+    def close(self):
+        self._h = None  # owned by the batch
+
+
+class Batch:
+    """Many instances advanced together (include/acogpu.h, aco_batch_*).
+
+    ``instances`` is a list of (x, y) coordinate arrays; instance i gets
+    min(num_ants, n_i) ants and seed params.seed + i * 0x9E3779B97F4A7C15.
+    """
+
+    def __init__(self, instances, params=None, num_ants=1024, **overrides):
+        L = lib()
+        self._L = L
+        self._h = None
+        p = params if params is not None else default_params()
+        p = AcoParams.from_buffer_copy(p)
+        p.num_ants = int(num_ants)
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        sizes = np.array([len(x) for x, _ in instances], dtype=np.int32)
+        coords = np.concatenate([np.concatenate([np.asarray(x, np.float32),
+                                                 np.asarray(y, np.float32)])
+                                 for x, y in instances]).astype(np.float32)
+        h = _vp()
+        st = L.aco_batch_create(ctypes.byref(p), len(sizes), _p(sizes, _i32p), _p(coords, _f32p),
+                                ctypes.byref(h))
+        if st != 0:
+            raise AcoError(st, "aco_batch_create: " + L.aco_status_string(st).decode())
+        self._h = h
+        self.sizes = sizes
+        self.params = p
+
+    def _check(self, st, what):
+        if st != 0:
+            msg = self._L.aco_batch_last_error(self._h).decode() if self._h else ""
+            raise AcoError(st, f"{what}: {msg or self._L.aco_status_string(st).decode()}")
+
+    def __len__(self):
+        return len(self.sizes)
+
+    def initialize(self):
+        self._check(self._L.aco_batch_initialize(self._h), "batch initialize")
+
+    def run(self, iterations):
+        self._check(self._L.aco_batch_run(self._h, int(iterations)), "batch run")
+
+    def synchronize(self):
+        self._check(self._L.aco_batch_synchronize(self._h), "batch synchronize")
+
+    def autotune(self):
+        t = _abi.AcoTuning()
+        self._check(self._L.aco_batch_autotune(self._h, ctypes.byref(t)), "batch autotune")
+        return {"ants_per_block": t.ants_per_block, "row_threads": t.row_threads,
+                "construct_ms": t.construct_ms, "rows_ms": t.rows_ms}
+
+    def set_tuning(self, ants_per_block, row_threads=0):
+        self._check(self._L.aco_batch_set_tuning(self._h, int(ants_per_block), int(row_threads)),
+                    "batch set_tuning")
+
+    def glob_best(self):
+        out = np.empty(len(self.sizes), dtype=np.int64)
+        self._check(self._L.aco_batch_get_glob_best(self._h, _p(out, _i64p)), "batch glob_best")
+        return out
+
+    def tours_built(self):
+        v = ctypes.c_int64()
+        self._check(self._L.aco_batch_get_tours_built(self._h, ctypes.byref(v)), "tours_built")
+        return v.value
+
+    def launch_count(self):
+        v = ctypes.c_int64()
+        self._check(self._L.aco_batch_get_launch_count(self._h, ctypes.byref(v)), "launches")
+        return v.value
+
+    def colony(self, i):
+        h = _vp()
+        self._check(self._L.aco_batch_get_colony(self._h, int(i), ctypes.byref(h)), "colony")
+        return _BorrowedColony(self._L, h, self.params)
+
+    def close(self):
+        if self._h:
+            self._L.aco_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

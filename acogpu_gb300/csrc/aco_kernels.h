@@ -43,10 +43,23 @@ cudaError_t launch_construct_staged(const ColonyDev &c, const int16_t *nn16, int
                                     cudaStream_t s);
 cudaError_t launch_nn_to_i16(const int32_t *nn, int n, int ldk, int16_t *nn16, cudaStream_t s);
 cudaError_t launch_epilogue(const ColonyDev &c, cudaStream_t s);
+
+// ---- batches of instances (descs: one ColonyDev per instance, in device memory) ----
+cudaError_t launch_batch_epilogue(const ColonyDev *descs, int count, cudaStream_t s);
+cudaError_t launch_batch_pheromone_rows(const ColonyDev *descs, const int2 *rowmap, int rows,
+                                        int max_ld, bool deposit_and_evaporate, cudaStream_t s,
+                                        int threads = 0);
+// Persistent construction over a queue of work items (instance, first ant, ants).
+size_t batch_construct_smem_bytes(int max_n, int max_k, int warps);
+cudaError_t configure_batch_construct(size_t smem);
+int batch_construct_blocks_per_sm(int warps, size_t smem, bool multi, bool aging);
+cudaError_t launch_batch_construct(const ColonyDev *descs, const int4 *items, int num_items,
+                                   int *queue_head, int grid, int warps, int max_n, int max_k,
+                                   bool aging, cudaStream_t s);
 // Row-owned pheromone pass: optional evaporation, optional ordered deposit
 // of the deposit list, then choice / choice_nn / tau_nn / row means.
 cudaError_t launch_pheromone_rows(const ColonyDev &c, bool evaporate, bool deposit,
-                                  bool write_tau, cudaStream_t s);
+                                  bool write_tau, cudaStream_t s, int threads = 0);
 // Atomic-mode pieces.
 cudaError_t launch_evaporate(const ColonyDev &c, cudaStream_t s);
 cudaError_t launch_deposit_atomic(const ColonyDev &c, cudaStream_t s);

@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <new>
 #include <string>
 #include <vector>
@@ -748,6 +749,350 @@ void aco_colony_destroy(aco_colony *c) {
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: many instances of uneven size advanced together.  Each instance
+// is a colony (same buffers, same initialisation); an iteration of the whole
+// batch is three launches over all instances -- a persistent construction
+// kernel fed by a work queue, one epilogue CTA per instance, one pheromone
+// CTA per row of every instance -- captured once into a CUDA graph.
+struct aco_batch {
+  aco_params p;
+  std::vector<aco_colony *> cols;
+  cudaStream_t stream = nullptr;
+  ColonyDev *d_descs = nullptr;
+  int2 *d_rowmap = nullptr;
+  int4 *d_items = nullptr;
+  int *d_queue = nullptr;
+  int total_rows = 0, num_items = 0;
+  int max_n = 0, max_k = 0, max_ld = 0, num_sms = 1;
+  int apb = 8, row_threads = 256, grid = 0;
+  bool initialized = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int bfail(aco_batch *b, int status, const std::string &msg) {
+  if (b) b->err = msg;
+  return status;
+}
+
+#define ACO_BCUDA(b, call, what)                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return bfail(b, e_ == cudaErrorMemoryAllocation ? ACO_ERR_OUT_OF_MEMORY : ACO_ERR_CUDA, \
+                   std::string(what) + ": " + cudaGetErrorString(e_));                   \
+  } while (0)
+
+void batch_drop_graph(aco_batch *b) {
+  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->graph_exec = nullptr;
+  b->graph = nullptr;
+}
+
+// Work items (instance, first ant, ants, 0), largest instances first.
+int batch_build_items(aco_batch *b) {
+  std::vector<int> order(b->cols.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int c) { return b->cols[a]->n > b->cols[c]->n; });
+  std::vector<int4> items;
+  for (int i : order) {
+    const int m = b->cols[i]->m;
+    for (int a0 = 0; a0 < m; a0 += b->apb) items.push_back(make_int4(i, a0, std::min(b->apb, m - a0), 0));
+  }
+  if (b->d_items) cudaFree(b->d_items);
+  b->d_items = nullptr;
+  ACO_BCUDA(b, cudaMalloc(&b->d_items, items.size() * sizeof(int4)), "alloc items");
+  ACO_BCUDA(b, cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(int4),
+                          cudaMemcpyHostToDevice),
+            "upload items");
+  b->num_items = (int)items.size();
+  const size_t smem = batch_construct_smem_bytes(b->max_n, b->max_k, b->apb);
+  ACO_BCUDA(b, configure_batch_construct(smem), "configure batch construct");
+  b->grid = b->num_sms * batch_construct_blocks_per_sm(b->apb, smem, b->max_k > 32,
+                                                       b->p.aging != 0);
+  batch_drop_graph(b);
+  return ACO_OK;
+}
+
+int batch_enqueue(aco_batch *b, bool construct, bool epilogue, bool rows, bool update) {
+  if (construct) {
+    ACO_BCUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream), "reset queue");
+    ACO_BCUDA(b, launch_batch_construct(b->d_descs, b->d_items, b->num_items, b->d_queue, b->grid,
+                                        b->apb, b->max_n, b->max_k, b->p.aging != 0, b->stream),
+              "batch construct");
+    b->launches++;
+  }
+  if (epilogue) {
+    ACO_BCUDA(b, launch_batch_epilogue(b->d_descs, (int)b->cols.size(), b->stream),
+              "batch epilogue");
+    b->launches++;
+  }
+  if (rows) {
+    ACO_BCUDA(b, launch_batch_pheromone_rows(b->d_descs, b->d_rowmap, b->total_rows, b->max_ld,
+                                             update, b->stream, b->row_threads),
+              "batch pheromone rows");
+    b->launches++;
+  }
+  return ACO_OK;
+}
+
+int batch_state_check(aco_batch *b) {
+  ACO_BCUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
+  for (aco_colony *c : b->cols) {
+    int s = device_error(c);
+    if (s) return bfail(b, s, c->err);
+  }
+  return ACO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int aco_batch_create(const aco_params *params, int32_t count, const int32_t *sizes,
+                     const float *coords, aco_batch **out) {
+  if (!out || !params || !sizes || !coords || count < 1) return ACO_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (params->deposit != ACO_DEPOSIT_DETERMINISTIC) return ACO_ERR_UNSUPPORTED;
+  aco_batch *b = new (std::nothrow) aco_batch();
+  if (!b) return ACO_ERR_OUT_OF_MEMORY;
+  b->p = *params;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete b;
+    return ACO_ERR_CUDA;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  size_t off = 0;
+  for (int32_t i = 0; i < count; i++) {
+    const int n = sizes[i];
+    aco_params pi = *params;
+    pi.num_ants = std::min(params->num_ants, n);
+    pi.seed = params->seed + (uint64_t)i * 0x9E3779B97F4A7C15ULL;
+    pi.construct_mode = ACO_CONSTRUCT_GLOBAL;
+    aco_colony *c = nullptr;
+    int s = aco_colony_create_coords(&pi, coords + off, coords + off + n, n, &c);
+    if (s) {
+      aco_batch_destroy(b);
+      return s;
+    }
+    aco_colony_set_stream(c, b->stream);
+    b->cols.push_back(c);
+    off += 2 * (size_t)n;
+    b->max_n = std::max(b->max_n, c->n);
+    b->max_k = std::max(b->max_k, c->K);
+    b->max_ld = std::max(b->max_ld, c->ld);
+    b->total_rows += n;
+  }
+  *out = b;
+  return ACO_OK;
+}
+
+int aco_batch_initialize(aco_batch *b) {
+  if (!b) return ACO_ERR_INVALID_ARGUMENT;
+  b->initialized = false;
+  batch_drop_graph(b);
+  std::vector<ColonyDev> descs;
+  std::vector<int2> rowmap;
+  for (size_t i = 0; i < b->cols.size(); i++) {
+    aco_colony *c = b->cols[i];
+    int s = aco_colony_initialize(c);
+    if (s) return bfail(b, s, c->err);
+    descs.push_back(make_dev(c));
+    for (int j = 0; j < c->n; j++) rowmap.push_back(make_int2((int)i, j));
+  }
+  if (!b->d_descs) {
+    ACO_BCUDA(b, cudaMalloc(&b->d_descs, descs.size() * sizeof(ColonyDev)), "alloc descs");
+    ACO_BCUDA(b, cudaMalloc(&b->d_rowmap, rowmap.size() * sizeof(int2)), "alloc rowmap");
+    ACO_BCUDA(b, cudaMalloc(&b->d_queue, sizeof(int)), "alloc queue");
+  }
+  ACO_BCUDA(b, cudaMemcpy(b->d_descs, descs.data(), descs.size() * sizeof(ColonyDev),
+                          cudaMemcpyHostToDevice),
+            "upload descs");
+  ACO_BCUDA(b, cudaMemcpy(b->d_rowmap, rowmap.data(), rowmap.size() * sizeof(int2),
+                          cudaMemcpyHostToDevice),
+            "upload rowmap");
+  ACO_BCUDA(b, configure_pheromone_rows(b->max_ld), "configure rows");
+  if (int s = batch_build_items(b)) return s;
+  b->initialized = true;
+  return ACO_OK;
+}
+
+int aco_batch_run(aco_batch *b, int32_t iterations) {
+  if (!b || iterations < 0) return ACO_ERR_INVALID_ARGUMENT;
+  if (!b->initialized) return bfail(b, ACO_ERR_NOT_INITIALIZED, "batch not initialized");
+  if (!b->graph_exec) {
+    const int64_t before = b->launches;
+    ACO_BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
+    int s = batch_enqueue(b, true, true, true, true);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (s) {
+      if (g) cudaGraphDestroy(g);
+      return s;
+    }
+    ACO_BCUDA(b, e, "end capture");
+    b->graph = g;
+    ACO_BCUDA(b, cudaGraphInstantiate(&b->graph_exec, g, 0), "instantiate");
+    b->launches = before;
+  }
+  for (int32_t i = 0; i < iterations; i++)
+    ACO_BCUDA(b, cudaGraphLaunch(b->graph_exec, b->stream), "graph launch");
+  b->launches += 3 * (int64_t)iterations;
+  return ACO_OK;
+}
+
+int aco_batch_synchronize(aco_batch *b) {
+  if (!b) return ACO_ERR_INVALID_ARGUMENT;
+  return batch_state_check(b);
+}
+
+int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
+  if (!b) return ACO_ERR_INVALID_ARGUMENT;
+  if (!b->initialized) return bfail(b, ACO_ERR_NOT_INITIALIZED, "batch not initialized");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int apbs[5] = {1, 2, 4, 8, 16};  // the kernel is launch-bounded to 512 threads
+  float best_ms = 1e30f;
+  int best_apb = b->apb;
+  for (int apb : apbs) {
+    if (batch_construct_smem_bytes(b->max_n, b->max_k, apb) > 200 * 1024) continue;
+    b->apb = apb;
+    if (int s = batch_build_items(b)) return s;
+    float ms = 1e30f;
+    for (int rep = 0; rep < 2; rep++) {
+      cudaEventRecord(e0, b->stream);
+      if (int s = batch_enqueue(b, true, false, false, false)) return s;
+      cudaEventRecord(e1, b->stream);
+      ACO_BCUDA(b, cudaEventSynchronize(e1), "tune construct");
+      float t = 0;
+      cudaEventElapsedTime(&t, e0, e1);
+      ms = std::min(ms, t);
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_apb = apb;
+    }
+  }
+  const int threads[3] = {128, 256, 512};
+  float best_rows = 1e30f;
+  int best_threads = b->row_threads;
+  for (int t : threads) {
+    b->row_threads = t;
+    float ms = 1e30f;
+    for (int rep = 0; rep < 2; rep++) {
+      cudaEventRecord(e0, b->stream);
+      if (int s = batch_enqueue(b, false, false, true, false)) return s;
+      cudaEventRecord(e1, b->stream);
+      ACO_BCUDA(b, cudaEventSynchronize(e1), "tune rows");
+      float v = 0;
+      cudaEventElapsedTime(&v, e0, e1);
+      ms = std::min(ms, v);
+    }
+    if (ms < best_rows) {
+      best_rows = ms;
+      best_threads = t;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->apb = best_apb;
+  b->row_threads = best_threads;
+  if (int s = batch_build_items(b)) return s;
+  // The timing runs advanced ages and counters: back to the initialised state.
+  for (aco_colony *c : b->cols) {
+    const ColonyDev d = make_dev(c);
+    ACO_BCUDA(b, launch_init_colony(d, b->stream), "reset");
+    ACO_BCUDA(b, launch_pheromone_rows(d, false, false, false, b->stream), "reset rows");
+  }
+  if (int s = batch_state_check(b)) return s;
+  if (out) {
+    memset(out, 0, sizeof(*out));
+    out->ants_per_block = best_apb;
+    out->row_threads = best_threads;
+    out->construct_ms = best_ms;
+    out->rows_ms = best_rows;
+  }
+  return ACO_OK;
+}
+
+int aco_batch_set_tuning(aco_batch *b, int32_t ants_per_block, int32_t row_threads) {
+  if (!b || ants_per_block < 1 || ants_per_block > 16 ||
+      (row_threads != 0 && (row_threads < 32 || row_threads > 512 || row_threads % 32)))
+    return ACO_ERR_INVALID_ARGUMENT;
+  b->apb = ants_per_block;
+  if (row_threads) b->row_threads = row_threads;
+  if (!b->initialized) return ACO_OK;
+  return batch_build_items(b);
+}
+
+int aco_batch_get_size(aco_batch *b, int32_t *count) {
+  if (!b || !count) return ACO_ERR_INVALID_ARGUMENT;
+  *count = (int32_t)b->cols.size();
+  return ACO_OK;
+}
+
+int aco_batch_get_colony(aco_batch *b, int32_t i, aco_colony **out) {
+  if (!b || !out || i < 0 || i >= (int32_t)b->cols.size()) return ACO_ERR_INVALID_ARGUMENT;
+  *out = b->cols[i];
+  return ACO_OK;
+}
+
+int aco_batch_get_glob_best(aco_batch *b, int64_t *out) {
+  if (!b || !out) return ACO_ERR_INVALID_ARGUMENT;
+  ACO_BCUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
+  for (size_t i = 0; i < b->cols.size(); i++) {
+    int s = aco_colony_get_glob_best(b->cols[i], &out[i]);
+    if (s) return bfail(b, s, b->cols[i]->err);
+  }
+  return ACO_OK;
+}
+
+int aco_batch_get_tours_built(aco_batch *b, int64_t *out) {
+  if (!b || !out) return ACO_ERR_INVALID_ARGUMENT;
+  int64_t total = 0;
+  for (aco_colony *c : b->cols) {
+    aco_stats st;
+    int s = aco_colony_get_stats(c, &st);
+    if (s) return bfail(b, s, c->err);
+    total += st.tours_built;
+  }
+  *out = total;
+  return ACO_OK;
+}
+
+int aco_batch_get_launch_count(aco_batch *b, int64_t *out) {
+  if (!b || !out) return ACO_ERR_INVALID_ARGUMENT;
+  *out = b->launches;
+  return ACO_OK;
+}
+
+const char *aco_batch_last_error(const aco_batch *b) { return b ? b->err.c_str() : ""; }
+
+void aco_batch_destroy(aco_batch *b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_drop_graph(b);
+  for (aco_colony *c : b->cols) aco_colony_destroy(c);
+  if (b->d_descs) cudaFree(b->d_descs);
+  if (b->d_rowmap) cudaFree(b->d_rowmap);
+  if (b->d_items) cudaFree(b->d_items);
+  if (b->d_queue) cudaFree(b->d_queue);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
 }
 
 }  // extern "C"

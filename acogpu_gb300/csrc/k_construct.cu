@@ -680,3 +680,96 @@ cudaError_t launch_construct_staged(const ColonyDev &c, const int16_t *nn16, int
 }
 
 }  // namespace aco
+
+namespace aco {
+
+// ---------------------------------------------------------------------------
+// Batches of instances of uneven size in one persistent launch.  Each CTA
+// takes work items -- (instance, first ant, ant count) -- from a global queue
+// with atomicAdd until the queue is empty; no CTA ever waits for another.
+// Items are ordered by decreasing instance size on the host (longest job
+// first), so the tail of the launch is made of small items.  The instance's
+// descriptor is copied into shared memory once per item.
+template <bool MULTI, bool AGING>
+__global__ void __launch_bounds__(512) k_batch_construct(const ColonyDev *__restrict__ descs,
+                                                         const int4 *__restrict__ items,
+                                                         int num_items, int *queue_head,
+                                                         int words, int max_chunks) {
+  extern __shared__ __align__(16) uint32_t smem_bc[];
+  __shared__ ColonyDev s_desc;
+  __shared__ int s_item;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *tabu = smem_bc + (size_t)warp * (words + 32 + (MULTI ? max_chunks : 0));
+  float *wbuf = reinterpret_cast<float *>(tabu + words);
+  float *cend = wbuf + 32;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(queue_head, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= num_items) break;
+    const int4 w = items[it];
+    if (threadIdx.x == 0) s_desc = descs[w.x];
+    __syncthreads();
+    const ColonyDev &c = s_desc;
+    if (warp < w.z)
+      construct_ant<MULTI, AGING, false>(c, w.y + warp, c.st->iteration, tabu, cend, wbuf,
+                                         nullptr, nullptr, nullptr, (c.K + 31) >> 5, lane);
+    __syncthreads();  // s_item and s_desc are rewritten by the next item
+  }
+}
+
+size_t batch_construct_smem_bytes(int max_n, int max_k, int warps) {
+  const int words = (max_n + 31) / 32;
+  const int chunks = (max_k + 31) / 32;
+  return (size_t)warps * (words + 32 + (max_k > 32 ? chunks : 0)) * 4;
+}
+
+cudaError_t configure_batch_construct(size_t smem) {
+  const int v = (int)smem;
+  const void *fns[4] = {(const void *)k_batch_construct<true, true>,
+                        (const void *)k_batch_construct<true, false>,
+                        (const void *)k_batch_construct<false, true>,
+                        (const void *)k_batch_construct<false, false>};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 4 && e == cudaSuccess; i++)
+    e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  return e;
+}
+
+int batch_construct_blocks_per_sm(int warps, size_t smem, bool multi, bool aging) {
+  int blocks = 0;
+  const void *f = multi ? (aging ? (const void *)k_batch_construct<true, true>
+                                 : (const void *)k_batch_construct<true, false>)
+                        : (aging ? (const void *)k_batch_construct<false, true>
+                                 : (const void *)k_batch_construct<false, false>);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, f, warps * 32, smem) != cudaSuccess)
+    return 1;
+  return blocks > 0 ? blocks : 1;
+}
+
+cudaError_t launch_batch_construct(const ColonyDev *descs, const int4 *items, int num_items,
+                                   int *queue_head, int grid, int warps, int max_n, int max_k,
+                                   bool aging, cudaStream_t s) {
+  const int words = (max_n + 31) / 32;
+  const int chunks = (max_k + 31) / 32;
+  const size_t smem = batch_construct_smem_bytes(max_n, max_k, warps);
+  const bool multi = max_k > 32;
+  if (multi) {
+    if (aging)
+      k_batch_construct<true, true><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
+                                                                  queue_head, words, chunks);
+    else
+      k_batch_construct<true, false><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
+                                                                   queue_head, words, chunks);
+  } else {
+    if (aging)
+      k_batch_construct<false, true><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
+                                                                   queue_head, words, chunks);
+    else
+      k_batch_construct<false, false><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
+                                                                    queue_head, words, chunks);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace aco

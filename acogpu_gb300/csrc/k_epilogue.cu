@@ -57,7 +57,7 @@ __device__ MinKey block_min(MinKey x, MinKey *scratch) {
   return r;
 }
 
-__global__ void __launch_bounds__(kEpiThreads) k_epilogue(ColonyDev c) {
+__device__ void epilogue_body(const ColonyDev &c) {
   __shared__ MinKey scratch[33];
   __shared__ uint32_t taken[kMaxRankAnts / 32];
   __shared__ int s_improved, s_best_ant;
@@ -184,9 +184,21 @@ __global__ void __launch_bounds__(kEpiThreads) k_epilogue(ColonyDev c) {
   if (tid == 0) st->iteration = st->iteration + 1;
 }
 
+__global__ void __launch_bounds__(kEpiThreads) k_epilogue(ColonyDev c) { epilogue_body(c); }
+
+// One CTA per instance of a batch.
+__global__ void __launch_bounds__(kEpiThreads) k_batch_epilogue(const ColonyDev *descs) {
+  epilogue_body(descs[blockIdx.x]);
+}
+
 cudaError_t launch_epilogue(const ColonyDev &c, cudaStream_t s) {
   if (c.m > kMaxRankAnts) return cudaErrorInvalidValue;
   k_epilogue<<<1, kEpiThreads, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_epilogue(const ColonyDev *descs, int count, cudaStream_t s) {
+  k_batch_epilogue<<<count, kEpiThreads, 0, s>>>(descs);
   return cudaGetLastError();
 }
 

@@ -35,9 +35,9 @@ __device__ __forceinline__ float choice_of(float tau, float eta, int use_alpha, 
 }
 
 template <bool EVAP, bool DEPOSIT, bool WRITE_TAU>
-__global__ void __launch_bounds__(kRowThreads) k_pheromone_rows(ColonyDev c) {
+__device__ __forceinline__ void pheromone_row_body(const ColonyDev &c, const int j) {
   extern __shared__ __align__(128) unsigned char smem_rows[];
-  const int ld = c.ld, n = c.n, tid = threadIdx.x, j = blockIdx.x;
+  const int ld = c.ld, n = c.n, tid = threadIdx.x, nthreads = blockDim.x;
   float *row = reinterpret_cast<float *>(smem_rows);
   float *erow = row + ld;
   uint32_t *mt = reinterpret_cast<uint32_t *>(erow + ld);
@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(kRowThreads) k_pheromone_rows(ColonyDev c) {
     fence_barrier_init();
   }
   if (DEPOSIT)
-    for (int h = tid; h < ld; h += kRowThreads) mt[h] = 0;
+    for (int h = tid; h < ld; h += nthreads) mt[h] = 0;
   __syncthreads();
   if (tid == 0) {
     const uint32_t bytes = (uint32_t)ld * 4u;
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(kRowThreads) k_pheromone_rows(ColonyDev c) {
   if (EVAP) {
     const float keep = __fsub_rn(1.0f, c.rho);
     const float fmin = min_pheromone();
-    for (int h = tid; h < n; h += kRowThreads) {
+    for (int h = tid; h < n; h += nthreads) {
       const float v = __fmul_rn(keep, row[h]);
       row[h] = v > fmin ? v : fmin;
     }
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kRowThreads) k_pheromone_rows(ColonyDev c) {
 
   float *trow = c.tau + (size_t)j * ld;
   float *crow = c.choice + (size_t)j * ld;
-  for (int h4 = tid; h4 < ld / 4; h4 += kRowThreads) {
+  for (int h4 = tid; h4 < ld / 4; h4 += nthreads) {
     const float4 t = reinterpret_cast<const float4 *>(row)[h4];
     const float4 e = reinterpret_cast<const float4 *>(erow)[h4];
     if (WRITE_TAU) reinterpret_cast<float4 *>(trow)[h4] = t;
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kRowThreads) k_pheromone_rows(ColonyDev c) {
     reinterpret_cast<float4 *>(crow)[h4] = cv;
   }
   const size_t koff = (size_t)j * c.ldk;
-  for (int r = tid; r < c.ldk; r += kRowThreads) {
+  for (int r = tid; r < c.ldk; r += nthreads) {
     float cv = 0.0f, tv = 0.0f;
     if (r < c.K) {
       const int id = c.nn[koff + r];
@@ -162,34 +162,72 @@ __global__ void __launch_bounds__(kRowThreads) k_pheromone_rows(ColonyDev c) {
   }
 }
 
+template <bool EVAP, bool DEPOSIT, bool WRITE_TAU>
+__global__ void __launch_bounds__(512) k_pheromone_rows(ColonyDev c) {
+  pheromone_row_body<EVAP, DEPOSIT, WRITE_TAU>(c, blockIdx.x);
+}
+
+// Batch form: global row g is row rowmap[g].y of instance rowmap[g].x.
+template <bool EVAP, bool DEPOSIT, bool WRITE_TAU>
+__global__ void __launch_bounds__(512) k_batch_pheromone_rows(const ColonyDev *descs,
+                                                            const int2 *rowmap) {
+  const int2 r = rowmap[blockIdx.x];
+  pheromone_row_body<EVAP, DEPOSIT, WRITE_TAU>(descs[r.x], r.y);
+}
+
 static size_t rows_smem(int ld, bool deposit) {
   return (size_t)ld * 4 * (deposit ? 3 : 2) + 32 * 4 + 16;
 }
 
+static int row_threads(int threads) { return threads > 0 ? threads : kRowThreads; }
+
 template <bool EVAP, bool DEPOSIT, bool WRITE_TAU>
-static cudaError_t launch_rows_t(const ColonyDev &c, cudaStream_t s) {
+static cudaError_t launch_rows_t(const ColonyDev &c, int threads, cudaStream_t s) {
   const size_t smem = rows_smem(c.ld, DEPOSIT);
-  k_pheromone_rows<EVAP, DEPOSIT, WRITE_TAU><<<c.n, kRowThreads, smem, s>>>(c);
+  k_pheromone_rows<EVAP, DEPOSIT, WRITE_TAU><<<c.n, row_threads(threads), smem, s>>>(c);
   return cudaGetLastError();
 }
 
+template <bool EVAP, bool DEPOSIT, bool WRITE_TAU>
+static cudaError_t configure_t(int ld) {
+  const int v = (int)rows_smem(ld, DEPOSIT);
+  cudaError_t e = cudaFuncSetAttribute(k_pheromone_rows<EVAP, DEPOSIT, WRITE_TAU>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_batch_pheromone_rows<EVAP, DEPOSIT, WRITE_TAU>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  return e;
+}
+
 cudaError_t configure_pheromone_rows(int ld) {
-  const int a = (int)rows_smem(ld, false), b = (int)rows_smem(ld, true);
-  cudaError_t e = cudaFuncSetAttribute(k_pheromone_rows<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pheromone_rows<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pheromone_rows<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pheromone_rows<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, a);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pheromone_rows<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, a);
+  cudaError_t e = configure_t<true, true, true>(ld);
+  if (e == cudaSuccess) e = configure_t<false, true, true>(ld);
+  if (e == cudaSuccess) e = configure_t<true, false, true>(ld);
+  if (e == cudaSuccess) e = configure_t<false, false, true>(ld);
+  if (e == cudaSuccess) e = configure_t<false, false, false>(ld);
   return e;
 }
 
 cudaError_t launch_pheromone_rows(const ColonyDev &c, bool evaporate, bool deposit,
-                                  bool write_tau, cudaStream_t s) {
-  if (evaporate && deposit) return launch_rows_t<true, true, true>(c, s);
-  if (evaporate) return launch_rows_t<true, false, true>(c, s);
-  if (deposit) return launch_rows_t<false, true, true>(c, s);
-  return write_tau ? launch_rows_t<false, false, true>(c, s)
-                   : launch_rows_t<false, false, false>(c, s);
+                                  bool write_tau, cudaStream_t s, int threads) {
+  if (evaporate && deposit) return launch_rows_t<true, true, true>(c, threads, s);
+  if (evaporate) return launch_rows_t<true, false, true>(c, threads, s);
+  if (deposit) return launch_rows_t<false, true, true>(c, threads, s);
+  return write_tau ? launch_rows_t<false, false, true>(c, threads, s)
+                   : launch_rows_t<false, false, false>(c, threads, s);
+}
+
+cudaError_t launch_batch_pheromone_rows(const ColonyDev *descs, const int2 *rowmap, int rows,
+                                        int max_ld, bool deposit_and_evaporate, cudaStream_t s,
+                                        int threads) {
+  const int t = row_threads(threads);
+  if (deposit_and_evaporate) {
+    k_batch_pheromone_rows<true, true, true><<<rows, t, rows_smem(max_ld, true), s>>>(descs, rowmap);
+  } else {
+    k_batch_pheromone_rows<false, false, false><<<rows, t, rows_smem(max_ld, false), s>>>(descs,
+                                                                                          rowmap);
+  }
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- atomic mode

@@ -311,6 +311,75 @@ def run_ours(args, rank, world, local):
     }
 
 
+BATCH_COUNT, BATCH_CAP, BATCH_K = 512, 1024, 20
+BATCH_WORKLOAD = ("512 instances, n log-uniform in [50,2000] (uniform and clustered alternating), "
+                  "m = min(n, 1024), k=20, AS, rho=0.1, beta=2; one persistent construction "
+                  "launch per iteration over a work queue, graph-replayed, autotuned")
+
+
+def batch_instances(count=BATCH_COUNT):
+    from acogpu_gb300 import instances
+    sizes = instances.batch_sizes(count, seed=7)
+    out = []
+    for i, n in enumerate(sizes):
+        gen = instances.uniform_instance if i % 2 == 0 else instances.clustered_instance
+        out.append(gen(int(n), seed=10_000 + i))
+    return out
+
+
+def batch_params():
+    from acogpu_gb300 import _abi
+    return _abi.default_params(num_ants=BATCH_CAP, cand_k=BATCH_K, rho=RHO, beta=BETA,
+                               nn_order=_abi.ACO_NN_STABLE, heuristic=_abi.ACO_HEURISTIC_DEVICE,
+                               fallback=_abi.ACO_FALLBACK_BEST, tau0_mode=_abi.ACO_TAU0_DORIGO,
+                               seed=4321)
+
+
+def run_batch(args, rank, world, local):
+    """Batched uneven instances: whole-batch iterations, device-timed."""
+    import torch
+    import acogpu_gb300 as aco
+    torch.cuda.set_device(local)
+    insts = batch_instances()
+    p = batch_params()
+    p.seed = 4321 + 7919 * rank
+    t0 = time.perf_counter()
+    b = aco.Batch(insts, params=p, num_ants=BATCH_CAP)
+    b.initialize()
+    tune = b.autotune()
+    setup_s = time.perf_counter() - t0
+    b.run(args.warmup)
+    b.synchronize()
+    built0, launches0 = b.tours_built(), b.launch_count()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start.record()
+        b.run(args.steps)
+        b.synchronize()
+        end.record()
+        torch.cuda.synchronize()
+    dev_s = start.elapsed_time(end) / 1e3
+    tours = b.tours_built() - built0
+    launches = b.launch_count() - launches0
+    sizes = np.array([len(x) for x, _ in insts])
+    ants = np.minimum(sizes, BATCH_CAP)
+    best = b.glob_best()
+    b.close()
+    if rank != 0:
+        return None
+    return {"metric": "tours/s", "value": tours / dev_s, "unit": "tours/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD, "instances": len(insts),
+                       "cities_total": int(sizes.sum()), "ants_per_iteration": int(ants.sum()),
+                       "l2": "working set 5+ GB, larger than L2"},
+            "ant_steps_per_s": float((ants * (sizes - 1)).sum()) * args.steps / dev_s,
+            "autotune": tune, "setup_s": setup_s, "gpu_launches": int(launches),
+            "mean_best_length": float(best.mean()), "clocks": clk.summary()}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -318,6 +387,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="rbas_aging_n1000", choices=("rbas_aging_n1000", "batch512"))
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
@@ -329,6 +399,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
+    if args.workload == "batch512":
+        out = run_batch(args, rank, world, local)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
     out = run_ours(args, rank, world, local)
     if out is not None:
         if not args.no_cpu_baseline:

@@ -247,6 +247,48 @@ ACO_API int aco_colony_set_stream(aco_colony *c, void *stream);
  * per replay). */
 ACO_API int aco_colony_get_launch_count(aco_colony *c, int64_t *out);
 
+/* ---- batches of instances ------------------------------------------------
+ * Many TSP instances of uneven size advanced together on one GPU: one
+ * iteration of the whole batch is a persistent construction launch fed by a
+ * per-instance work queue, one epilogue CTA per instance and one pheromone
+ * CTA per row, captured once into a CUDA graph.  The reference runs one
+ * instance per process (src/Setup.cpp:73-129); this has no counterpart there
+ * and exists for throughput on many instances.  Instance i gets
+ * m_i = min(params->num_ants, n_i) ants and seed params->seed + i*0x9E3779B97F4A7C15,
+ * and evolves exactly like a colony created with those parameters.
+ * coords: for each instance in turn, its n_i x values then its n_i y values.
+ * Only ACO_DEPOSIT_DETERMINISTIC is supported. */
+typedef struct aco_batch aco_batch;
+
+typedef struct aco_tuning {
+  int32_t ants_per_block; /* warps (ants) per CTA of the construction launch */
+  int32_t row_threads;    /* threads per CTA of the pheromone row pass */
+  float construct_ms;     /* best timed construction launch */
+  float rows_ms;          /* best timed row pass */
+  int32_t reserved[4];
+} aco_tuning;
+
+ACO_API int aco_batch_create(const aco_params *params, int32_t count, const int32_t *sizes,
+                             const float *coords, aco_batch **out);
+ACO_API int aco_batch_initialize(aco_batch *b);
+/* `iterations` graph-replayed iterations of every instance, asynchronous. */
+ACO_API int aco_batch_run(aco_batch *b, int32_t iterations);
+ACO_API int aco_batch_synchronize(aco_batch *b);
+/* Times the construction launch for 1..16 ants per CTA and the row pass for
+ * 128..512 threads, keeps the fastest, then returns every instance to its
+ * initialised state.  Call after aco_batch_initialize, before running. */
+ACO_API int aco_batch_autotune(aco_batch *b, aco_tuning *out);
+ACO_API int aco_batch_set_tuning(aco_batch *b, int32_t ants_per_block, int32_t row_threads);
+ACO_API int aco_batch_get_size(aco_batch *b, int32_t *count);
+/* Borrowed handle of instance i (read its state with the colony getters;
+ * do not destroy or run it). */
+ACO_API int aco_batch_get_colony(aco_batch *b, int32_t i, aco_colony **out);
+ACO_API int aco_batch_get_glob_best(aco_batch *b, int64_t *out_count);
+ACO_API int aco_batch_get_tours_built(aco_batch *b, int64_t *out);
+ACO_API int aco_batch_get_launch_count(aco_batch *b, int64_t *out);
+ACO_API const char *aco_batch_last_error(const aco_batch *b);
+ACO_API void aco_batch_destroy(aco_batch *b);
+
 /* Largest city count accepted by aco_nn_list_reference_order_noalloc. */
 #define ACO_NOALLOC_MAX_CITIES 1024
 
