@@ -20,39 +20,7 @@
 
 using namespace aco;
 
-struct aco_colony {
-  aco_params p;
-  int n = 0, m = 0, K = 0, ld = 0, ldk = 0, ldm = 0;
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  int32_t *dist = nullptr;
-  float *eta = nullptr, *tau = nullptr, *choice = nullptr;
-  int32_t *nn = nullptr;
-  float *eta_nn = nullptr, *tau_nn = nullptr, *choice_nn = nullptr;
-  int32_t *tours = nullptr;
-  int64_t *newlen = nullptr, *len = nullptr;
-  int32_t *succT = nullptr, *predT = nullptr, *gbtour = nullptr;
-  int32_t *age = nullptr, *perf = nullptr;
-  uint8_t *valid = nullptr;
-  float *mean = nullptr;
-  int32_t *dep_col = nullptr;
-  float *dep_delta = nullptr;
-  ColonyState *st = nullptr;
-  int16_t *nn16 = nullptr;  // candidate ids as int16, 32 per row (staged kernel)
-  bool staged = false;
-  int staged_grid = 0, staged_warps = 0;
-  int num_sms = 0, max_smem_optin = 0;
-  std::vector<void *> allocations;
-  bool initialized = false;
-  int64_t optimum = -1;
-  int apb = 4;
-  int64_t launches = 0;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t graph_exec = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  std::string err;
-};
+#include "colony_internal.h"
 
 namespace {
 
@@ -204,6 +172,15 @@ int create_common(const aco_params *params, int32_t n, aco_colony **out, aco_col
   return ACO_OK;
 }
 
+}  // namespace
+
+ColonyDev aco::colony_dev(const aco_colony *c) { return make_dev(c); }
+int aco::colony_fail(aco_colony *c, int status, const std::string &msg) {
+  return fail(c, status, msg);
+}
+
+namespace {
+
 int device_error(aco_colony *c) {
   ColonyState h;
   ACO_CUDA(c, cudaMemcpyAsync(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost, c->stream),
@@ -341,13 +318,16 @@ int aco_colony_create_coords(const aco_params *params, const float *x, const flo
   aco_colony *c = nullptr;
   int s = create_common(params, n, out, &c);
   if (s) return s;
-  float *dxy = nullptr;
-  cudaError_t e = cudaMallocAsync(&dxy, (size_t)2 * n * 4, c->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dxy, x, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+  // The coordinates stay on the device: the learned prior's features use them.
+  if ((s = dalloc(c, &c->xy, (size_t)2 * n))) {
+    aco_colony_destroy(c);
+    return s;
+  }
+  float *dxy = c->xy;
+  cudaError_t e = cudaMemcpyAsync(dxy, x, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(dxy + n, y, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = launch_distances_from_coords(dxy, dxy + n, n, c->ld, c->dist, c->stream);
-  if (dxy) cudaFreeAsync(dxy, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
     aco_colony_destroy(c);
@@ -644,6 +624,11 @@ int aco_colony_read_nn_list(aco_colony *c, int32_t *out) {
   if (!c) return ACO_ERR_INVALID_ARGUMENT;
   return read_matrix_f32(c, reinterpret_cast<const float *>(c->nn), c->K, c->ldk,
                          reinterpret_cast<float *>(out));
+}
+
+int aco_colony_read_candidate_heuristic(aco_colony *c, float *out) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  return read_matrix_f32(c, c->eta_nn, c->K, c->ldk, out);
 }
 
 int aco_colony_read_distances(aco_colony *c, int32_t *out) {

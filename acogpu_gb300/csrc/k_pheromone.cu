@@ -150,7 +150,9 @@ __device__ __forceinline__ void pheromone_row_body(const ColonyDev &c, const int
     if (r < c.K) {
       const int id = c.nn[koff + r];
       tv = row[id];
-      cv = choice_of(tv, erow[id], c.use_alpha, c.alpha);
+      // eta_nn is eta gathered in candidate order (times the learned prior,
+      // when one is installed), so without a prior this is tau * eta.
+      cv = choice_of(tv, c.eta_nn[koff + r], c.use_alpha, c.alpha);
     }
     c.choice_nn[koff + r] = cv;
     if (c.aging) c.tau_nn[koff + r] = tv;

@@ -289,6 +289,44 @@ ACO_API int aco_batch_get_launch_count(aco_batch *b, int64_t *out);
 ACO_API const char *aco_batch_last_error(const aco_batch *b);
 ACO_API void aco_batch_destroy(aco_batch *b);
 
+/* ---- learned heuristic prior ------------------------------------------------
+ * An edge-scoring MLP (12 features per candidate edge -> 128 -> 128 -> 1,
+ * ReLU, logistic output; BF16 tensor-core GEMMs with FP32 accumulation) that
+ * predicts whether a candidate edge lies on the best tour the plain method
+ * finds.  Its output p multiplies the candidate heuristic of a colony:
+ * eta'_ir = eta_ir * (floor + p).  No counterpart in the reference.
+ * Features of edge i -> j = nn[i][r] (distances d, K = candidate count):
+ *   d/dK_i, d/dK_j, r/K, rank of i in j's list / K (1 if absent),
+ *   (x_j-x_i)/dK_i, (y_j-y_i)/dK_i, d1_i/dK_i, d1_j/dK_j, d/(d1_i+d1_j+1),
+ *   dK_i/mean dK, dK_j/mean dK, mutual top-5 flag
+ * (dK = distance to the K-th candidate, d1 = to the nearest).
+ * Parameters are packed as W1[128][12] b1[128] W2[128][128] b2[128] w3[128] b3. */
+typedef struct aco_prior aco_prior;
+ACO_API int aco_prior_create(uint64_t seed, aco_prior **out);
+ACO_API int aco_prior_param_count(void);
+ACO_API int aco_prior_get_weights(aco_prior *p, float *out);
+ACO_API int aco_prior_set_weights(aco_prior *p, const float *in);
+/* Appends the candidate edges of an initialized colony built from
+ * coordinates, labelled by its best-so-far tour. */
+ACO_API int aco_prior_add_examples(aco_prior *p, aco_colony *c);
+ACO_API int aco_prior_num_examples(aco_prior *p, int64_t *examples, int64_t *positives);
+ACO_API int aco_prior_clear_examples(aco_prior *p);
+/* Adam on the weighted logistic loss (positives weighted by #neg/#pos). */
+ACO_API int aco_prior_train(aco_prior *p, int32_t epochs, int32_t batch, float lr, uint64_t seed,
+                            float *last_loss);
+/* Loss and packed gradient of a batch given on the host (E x 12 features). */
+ACO_API int aco_prior_loss_and_grads(aco_prior *p, const float *feats, const float *labels,
+                                     int32_t E, float pos_weight, float *loss, float *grads);
+ACO_API int aco_prior_predict(aco_prior *p, const float *feats, int32_t E, float *probs);
+/* Scores the colony's candidate edges and installs the prior. */
+ACO_API int aco_prior_apply(aco_prior *p, aco_colony *c, float floor);
+ACO_API const char *aco_prior_last_error(const aco_prior *p);
+ACO_API void aco_prior_destroy(aco_prior *p);
+/* Features of every candidate edge of a colony built from coordinates
+ * (n*k rows of 12, row i*k + r), and its candidate heuristic (n*k). */
+ACO_API int aco_colony_edge_features(aco_colony *c, float *out);
+ACO_API int aco_colony_read_candidate_heuristic(aco_colony *c, float *out_nk);
+
 /* Largest city count accepted by aco_nn_list_reference_order_noalloc. */
 #define ACO_NOALLOC_MAX_CITIES 1024
 

@@ -170,6 +170,10 @@ class Port:
     def heuristic(self):
         return self._nn_f(self.L.oc_get_heuristic)
 
+    def set_candidate_heuristic(self, eta_nk):
+        eta_nk = np.ascontiguousarray(eta_nk, dtype=np.float32)
+        self.L.oc_set_candidate_heuristic(self.h, _ptr(eta_nk, _f32p))
+
     def choice(self):
         return self._nn_f(self.L.oc_get_choice)
 

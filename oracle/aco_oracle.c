@@ -182,6 +182,9 @@ struct oc_colony {
   uint8_t *valid;
   float *mean;
   int32_t num_valid, isconverged, globalperformance;
+  /* candidate heuristic (n*k, candidate order) when a learned prior is
+   * installed; NULL: the plain heuristic */
+  float *eta_nn;
   /* deposit list of the current iteration */
   int32_t *dep_src; /* ant index, or -1 for the best-so-far tour */
   float *dep_delta;
@@ -228,7 +231,7 @@ void oc_destroy(oc_colony *c) {
   free(c->dist); free(c->nn); free(c->eta); free(c->tau); free(c->choice);
   free(c->tour); free(c->newlen); free(c->len); free(c->gbtour);
   free(c->age); free(c->perf); free(c->valid); free(c->mean);
-  free(c->dep_src); free(c->dep_delta);
+  free(c->dep_src); free(c->dep_delta); free(c->eta_nn);
   free(c);
 }
 
@@ -313,6 +316,25 @@ static float fitness(const oc_colony *c, int32_t cur, int32_t city, int32_t ant)
   return p * c->eta[xy];
 }
 
+/* Weight of candidate r (city `city`) of row `cur`: the fitness with the
+ * candidate heuristic in place of eta when a prior is installed. */
+static float cand_fitness(const oc_colony *c, int32_t cur, int32_t r, int32_t city, int32_t ant) {
+  if (!c->eta_nn) return fitness(c, cur, city, ant);
+  const int64_t xy = (int64_t)cur * c->n + city;
+  float p = c->tau[xy];
+  if (c->p.aging && c->age[ant] < c->p.min_retirement_age && c->isconverged) {
+    float ratio = (float)c->age[ant] / (float)c->p.min_retirement_age;
+    p = ((p - c->mean[cur]) * ratio) + c->mean[cur];
+  }
+  if (c->p.use_alpha) p = powf(p, c->p.alpha);
+  return p * c->eta_nn[(int64_t)cur * c->k + r];
+}
+
+void oc_set_candidate_heuristic(oc_colony *c, const float *eta_nk) {
+  if (!c->eta_nn) c->eta_nn = (float *)malloc(sizeof(float) * (size_t)c->n * c->k);
+  memcpy(c->eta_nn, eta_nk, sizeof(float) * (size_t)c->n * c->k);
+}
+
 /* select_local_best, inc/Colony.cuh:33-43: index of the last unvisited city
  * of the full nn row. */
 static int32_t last_unvisited(const oc_colony *c, const int32_t *nnrow, const uint8_t *vis) {
@@ -359,7 +381,7 @@ static void construct_ant(oc_colony *c, int32_t k, float *w, uint8_t *vis, int64
     float sum = 0;
     for (int32_t i = 0; i < K; i++) {
       int32_t city = row[i];
-      w[i] = vis[city] ? 0.0f : fitness(c, cur, city, k);
+      w[i] = vis[city] ? 0.0f : cand_fitness(c, cur, i, city, k);
       sum += w[i];
     }
     int32_t next;

@@ -57,6 +57,9 @@ void oc_get_lengths(const oc_colony *c, int64_t *out);
 void oc_get_best_tour(const oc_colony *c, int32_t *out);
 void oc_get_aging(const oc_colony *c, int32_t *age, int32_t *perf, uint8_t *valid,
                   float *mean, int32_t *misc);
+/* Installs a candidate heuristic (n*k, candidate order), as the GPU does
+ * when a learned prior is applied; the fallback keeps the plain one. */
+void oc_set_candidate_heuristic(oc_colony *c, const float *eta_nk);
 /* Fallback decisions taken in the last iteration (steps where the candidate
  * roulette could not pick a city). */
 int64_t oc_fallback_count(const oc_colony *c);

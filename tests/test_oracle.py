@@ -182,3 +182,23 @@ def test_rank_based_update_uses_ranked_ants_and_best_so_far():
     ref64 = oracle.pheromone_update_f64(tau0, 0.25, np.stack(srcs), np.array(ls), np.array(w))
     tau = q.pheromone().astype(np.float64)
     assert np.max(np.abs(tau - ref64) / ref64) < 1e-5
+
+
+def test_mlp_oracle_backward_matches_finite_differences():
+    """The MLP oracle's analytic gradient (exact arithmetic) against central
+    differences of its own loss."""
+    from oracle import mlp_oracle as mo
+    rng = np.random.default_rng(3)
+    X = rng.normal(size=(40, 12))
+    y = (rng.random(40) < 0.3).astype(np.float64)
+    w = np.concatenate([rng.normal(size=128 * 12) * 0.3, rng.normal(size=128) * 0.1,
+                        rng.normal(size=128 * 128) * 0.1, rng.normal(size=128) * 0.1,
+                        rng.normal(size=128) * 0.2, [0.05]])
+    loss, g = mo.loss_and_grads(w, X, y, pos_weight=3.0, exact=True)
+    idx = rng.choice(len(w), 60, replace=False)
+    for i in idx:
+        e = np.zeros_like(w)
+        e[i] = 1e-6
+        num = (mo.loss_and_grads(w + e, X, y, 3.0, True)[0] -
+               mo.loss_and_grads(w - e, X, y, 3.0, True)[0]) / 2e-6
+        assert abs(num - g[i]) <= 1e-6 + 1e-4 * abs(num), (i, num, g[i])
