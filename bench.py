@@ -380,6 +380,158 @@ def run_batch(args, rank, world, local):
             "mean_best_length": float(best.mean()), "clocks": clk.summary()}
 
 
+def run_large(args, rank, world, local):
+    """Large single instance: n=4096 uniform in [0,100000)^2, m=512, k=32,
+    atomic deposit, plain AS (configs[2])."""
+    import torch
+    import acogpu_gb300 as aco
+    from acogpu_gb300 import _abi, instances
+    torch.cuda.set_device(local)
+    x, y = instances.uniform_instance(4096, box=100000, seed=4096)
+    p = _abi.default_params(num_ants=512, cand_k=32, rho=RHO, beta=BETA,
+                            nn_order=_abi.ACO_NN_STABLE, heuristic=_abi.ACO_HEURISTIC_DEVICE,
+                            fallback=_abi.ACO_FALLBACK_BEST, tau0_mode=_abi.ACO_TAU0_DORIGO,
+                            deposit=_abi.ACO_DEPOSIT_ATOMIC, seed=77 + rank)
+    col = aco.Colony(coords=(x, y), params=p, num_ants=512)
+    col.initialize()
+    for _ in range(args.warmup):
+        col.constructSolution()
+    col.synchronize()
+    st0, l0 = col.stats(), col.launch_count()
+    stage = np.zeros(6)
+    ms = 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t = col.constructSolution(timers=True)
+            stage += t
+            ms += float(t.sum())
+    st1 = col.stats()
+    tours = st1["tours_built"] - st0["tours_built"]
+    fallbacks = st1["fallbacks"] - st0["fallbacks"]
+    bytes_c = construct_bytes(4096, 32, tours, fallbacks)
+    hbm = peaks().get("hbm_gbs")
+    achieved = bytes_c / (stage[1] / 1e3) / 1e9
+    best = col.getGlobBestDist()
+    launches = col.launch_count() - l0
+    col.close()
+    if rank != 0:
+        return None
+    return {"metric": "tours/s", "value": tours / (ms / 1e3), "unit": "tours/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "plain AS, n=4096 uniform in [0,100000)^2, m=512, k=32, "
+                       "rho=0.1, atomic deposit", "n": 4096, "m": 512, "k": 32,
+                       "l2": "tau/eta/choice 3 x 64 MB + dist 64 MB > L2"},
+            "stage_ms_per_step": {"construct": stage[1] / args.steps,
+                                  "epilogue": stage[2] / args.steps,
+                                  "pheromone": stage[4] / args.steps},
+            "fallback_rate": fallbacks / max(1, tours * 4095), "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "k_construct", "achieved": achieved,
+                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None},
+            "best": best, "clocks": clk.summary()}
+
+
+def _batch_timed(b, iters, chunk):
+    """Runs `iters` batch iterations in chunks; returns [(gpu_s, mean best)]."""
+    import torch
+    trace, total = [], 0.0
+    done = 0
+    while done < iters:
+        step = min(chunk, iters - done)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s.record()
+        b.run(step)
+        b.synchronize()
+        e.record()
+        torch.cuda.synchronize()
+        total += s.elapsed_time(e) / 1e3
+        done += step
+        trace.append((total, float(b.glob_best().mean()), done))
+    return trace
+
+
+def run_learned(args, rank, world, local):
+    """Learned prior vs plain ACO at equal GPU time (scaled-down C5)."""
+    import torch
+    import acogpu_gb300 as aco
+    from acogpu_gb300 import instances
+    from acogpu_gb300.prior import EdgePrior
+    torch.cuda.set_device(local)
+    g = instances.SplitMix64(31)
+    train_sizes = (100 + g.integers(args.train_instances, 401)).astype(int)
+    train = [instances.uniform_instance(int(n), seed=20_000 + i) if i % 2 == 0 else
+             instances.clustered_instance(int(n), seed=20_000 + i)
+             for i, n in enumerate(train_sizes)]
+    p = batch_params()
+    t0 = time.perf_counter()
+    b = aco.Batch(train, params=p, num_ants=BATCH_CAP)
+    b.initialize()
+    b.run(args.train_iters)
+    b.synchronize()
+    prior = EdgePrior(seed=17)
+    for i in range(len(train)):
+        prior.add_examples(b.colony(i))
+    examples, positives = prior.num_examples()
+    b.close()
+    loss0 = prior.train(epochs=1, batch=65536, lr=2e-3, seed=1)
+    loss = prior.train(epochs=args.epochs, batch=65536, lr=1e-3, seed=2)
+    train_s = time.perf_counter() - t0
+
+    sizes = instances.batch_sizes(args.eval_instances, lo=200, hi=2000, seed=41)
+    evals = [instances.uniform_instance(int(n), seed=30_000 + i) if i % 2 == 0 else
+             instances.clustered_instance(int(n), seed=30_000 + i) for i, n in enumerate(sizes)]
+    plain = aco.Batch(evals, params=p, num_ants=BATCH_CAP)
+    plain.initialize()
+    plain.autotune()
+    plain_trace = _batch_timed(plain, args.plain_iters, 50)
+    plain.close()
+    t_plain, best_plain = plain_trace[-1][0], plain_trace[-1][1]
+
+    learned = aco.Batch(evals, params=p, num_ants=BATCH_CAP)
+    learned.initialize()
+    learned.autotune()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record()
+    for i in range(len(evals)):
+        prior.apply(learned.colony(i), floor=0.05)
+    e.record()
+    torch.cuda.synchronize()
+    t_infer = s.elapsed_time(e) / 1e3
+    budget = 0.25 * t_plain - t_infer
+    trace, spent, done = [], 0.0, 0
+    chunk = 10
+    while spent < budget and done < args.plain_iters:
+        tr = _batch_timed(learned, chunk, chunk)
+        spent += tr[-1][0]
+        done += chunk
+        trace.append((t_infer + spent, tr[-1][1], done))
+    learned.close()
+    prior.close()
+    best_learned = trace[-1][1] if trace else float("nan")
+    reach = next((t for t, v, _ in trace if v <= best_plain * 1.001), None)
+    if rank != 0:
+        return None
+    return {"metric": "tour-length gap at equal GPU time (learned prior vs plain)",
+            "value": 100.0 * (best_learned - best_plain) / best_plain, "unit": "%",
+            "higher_is_better": False, "n_gpus": world, "data": "synthetic", "dtype": "bf16+f32",
+            "config": {"workload": "learned edge prior, scaled-down: "
+                       f"{len(train)} training instances n in [100,500] labelled by "
+                       f"{args.train_iters}-iteration plain best tours; {len(evals)} evaluation "
+                       f"instances n log-uniform [200,2000]; plain {args.plain_iters} iterations "
+                       "vs learned at 25% of plain's GPU time", "k": BATCH_K,
+                       "ants_cap": BATCH_CAP},
+            "plain": {"gpu_s": t_plain, "iterations": args.plain_iters, "mean_best": best_plain,
+                      "trace": plain_trace[::max(1, len(plain_trace) // 10)]},
+            "learned": {"gpu_s": trace[-1][0] if trace else None, "iterations": done,
+                        "inference_s": t_infer, "mean_best": best_learned,
+                        "reaches_plain_within_0.1pct_at_s": reach},
+            "training": {"examples": examples, "positives": positives, "loss_first_epoch": loss0,
+                         "loss_last_epoch": loss, "wall_s": train_s}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -387,7 +539,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="rbas_aging_n1000", choices=("rbas_aging_n1000", "batch512"))
+    ap.add_argument("--workload", default="rbas_aging_n1000",
+                    choices=("rbas_aging_n1000", "batch512", "learned", "large4096"))
+    ap.add_argument("--train-instances", type=int, default=1024)
+    ap.add_argument("--train-iters", type=int, default=200)
+    ap.add_argument("--eval-instances", type=int, default=256)
+    ap.add_argument("--plain-iters", type=int, default=1000)
+    ap.add_argument("--epochs", type=int, default=4)
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
@@ -399,8 +557,9 @@ def main():
         import torch
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
-    if args.workload == "batch512":
-        out = run_batch(args, rank, world, local)
+    if args.workload in ("batch512", "learned", "large4096"):
+        fn = {"batch512": run_batch, "learned": run_learned, "large4096": run_large}[args.workload]
+        out = fn(args, rank, world, local)
         if out is not None:
             print(json.dumps(out), flush=True)
         return
