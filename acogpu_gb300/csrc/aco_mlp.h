@@ -28,6 +28,12 @@ cudaError_t launch_edge_features(const ColonyDev &c, const float *x, const float
 cudaError_t launch_gemm_tn(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb,
                            float *C, int ldc, int M, int N, int K, int mode, int splits,
                            cudaStream_t s);
+// The same product on the 5th-generation tensor cores (tcgen05 + TMA);
+// N must be 128 or 16, A and B 16-byte aligned.  err: device word for
+// timeout flags (may be null).
+cudaError_t launch_gemm_tn_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb,
+                              float *C, int ldc, int M, int N, int K, int mode, int splits,
+                              uint32_t *err, cudaStream_t s);
 cudaError_t launch_bias_relu(const float *Z, const float *bias, int E, int Hd,
                              __nv_bfloat16 *Hout, __nv_bfloat16 *Ht, int ldt, cudaStream_t s);
 cudaError_t launch_head(const __nv_bfloat16 *H2, const float *w3, const float *b3, int E,

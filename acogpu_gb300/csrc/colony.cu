@@ -300,8 +300,12 @@ int aco_colony_create(const aco_params *params, const int32_t *dist, int32_t n,
     cudaGetLastError();  // clear a possible "invalid value" from a plain host pointer
   }
   const cudaMemcpyKind kind = dist_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  cudaError_t e = cudaMemcpy2DAsync(c->dist, (size_t)c->ld * 4, dist, (size_t)n * 4,
-                                    (size_t)n * 4, n, kind, c->stream);
+  // A device matrix may still be in flight on the caller's stream, which the
+  // colony's non-blocking stream is not ordered after: wait for it once.
+  cudaError_t e = dist_on_device ? cudaDeviceSynchronize() : cudaSuccess;
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(c->dist, (size_t)c->ld * 4, dist, (size_t)n * 4, (size_t)n * 4, n, kind,
+                          c->stream);
   if (e == cudaSuccess) e = launch_fill_padding_int(c->dist, n, c->ld, ACO_MAX_DISTANCE, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
@@ -784,6 +788,14 @@ void batch_drop_graph(aco_batch *b) {
   b->graph = nullptr;
 }
 
+// Host -> device upload on the batch's own stream.  The stream is
+// non-blocking, so a plain cudaMemcpy (legacy stream; a pageable upload may
+// return before its DMA lands) would not be ordered before the next launch.
+cudaError_t upload_sync(aco_batch *b, void *dst, const void *src, size_t bytes) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, b->stream);
+  return e == cudaSuccess ? cudaStreamSynchronize(b->stream) : e;
+}
+
 // Work items (instance, first ant, ants, 0), largest instances first.
 int batch_build_items(aco_batch *b) {
   std::vector<int> order(b->cols.size());
@@ -798,8 +810,7 @@ int batch_build_items(aco_batch *b) {
   if (b->d_items) cudaFree(b->d_items);
   b->d_items = nullptr;
   ACO_BCUDA(b, cudaMalloc(&b->d_items, items.size() * sizeof(int4)), "alloc items");
-  ACO_BCUDA(b, cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(int4),
-                          cudaMemcpyHostToDevice),
+  ACO_BCUDA(b, upload_sync(b, b->d_items, items.data(), items.size() * sizeof(int4)),
             "upload items");
   b->num_items = (int)items.size();
   const size_t smem = batch_construct_smem_bytes(b->max_n, b->max_k, b->apb);
@@ -903,11 +914,9 @@ int aco_batch_initialize(aco_batch *b) {
     ACO_BCUDA(b, cudaMalloc(&b->d_rowmap, rowmap.size() * sizeof(int2)), "alloc rowmap");
     ACO_BCUDA(b, cudaMalloc(&b->d_queue, sizeof(int)), "alloc queue");
   }
-  ACO_BCUDA(b, cudaMemcpy(b->d_descs, descs.data(), descs.size() * sizeof(ColonyDev),
-                          cudaMemcpyHostToDevice),
+  ACO_BCUDA(b, upload_sync(b, b->d_descs, descs.data(), descs.size() * sizeof(ColonyDev)),
             "upload descs");
-  ACO_BCUDA(b, cudaMemcpy(b->d_rowmap, rowmap.data(), rowmap.size() * sizeof(int2),
-                          cudaMemcpyHostToDevice),
+  ACO_BCUDA(b, upload_sync(b, b->d_rowmap, rowmap.data(), rowmap.size() * sizeof(int2)),
             "upload rowmap");
   ACO_BCUDA(b, configure_pheromone_rows(b->max_ld), "configure rows");
   if (int s = batch_build_items(b)) return s;

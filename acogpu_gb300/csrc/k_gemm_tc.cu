@@ -1,0 +1,293 @@
+// k_gemm_tc.cu -- BF16 "TN" GEMM on the 5th-generation tensor cores:
+// C[M x N] (op)= A[M x K] * B[N x K]^T, A and B K-contiguous, FP32 C.
+//
+// One CTA (4 warps) computes a 128 x BN tile:
+//  * thread 0 stages each 64-wide K block of A (128 x 64) and B (BN x 64)
+//    into shared memory with 2-D TMA loads (cp.async.bulk.tensor, 128-byte
+//    swizzle; rows and columns outside the tensors read as zero) on an
+//    mbarrier;
+//  * it issues four tcgen05.mma.kind::f16 (M=128, N=BN, K=16 each) with
+//    the accumulator in tensor memory, then tcgen05.commit to a second
+//    mbarrier, which also frees the staging buffers for the next block;
+//  * warp w reads accumulator lanes 32w..32w+31 with tcgen05.ld and writes
+//    (or atomically adds, for split K) its rows of C.
+// Tensor memory is allocated by warp 0 and released on every path; every
+// wait is bounded and reports a timeout through the error word.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include "aco_kernels.h"
+#include "aco_mlp.h"
+
+namespace aco {
+
+namespace {
+
+constexpr int kTcBM = 128, kTcBK = 64;
+
+// Bounded mbarrier wait (see mbar_wait_bounded) reporting into `err`.
+__device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err) {
+  for (uint32_t i = 0; i < kMaxPolls; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicOr(err, kErrTimeout);
+  return false;
+}
+
+// Shared-memory descriptor of a K-major operand tile with 128-byte
+// swizzle: start address, stride between 8-row groups (1024 bytes),
+// descriptor version 1, layout type SWIZZLE_128B.
+__device__ __forceinline__ uint64_t smem_desc_sw128(const void *tile) {
+  const uint64_t addr = smem_u32(tile);
+  uint64_t d = (addr >> 4) & 0x3FFFull;
+  d |= 1ull << 16;                   // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+  d |= 1ull << 46;                   // version
+  d |= 2ull << 61;                   // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTcBM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
+      "{%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+template <int NCOL>
+__device__ __forceinline__ void tmem_load_32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_load_16(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_gemm_tn_tc(const __grid_constant__ CUtensorMap tmA,
+                                                    const __grid_constant__ CUtensorMap tmB,
+                                                    float *__restrict__ C, int ldc, int M, int N,
+                                                    int K, int k_per_split, int mode,
+                                                    uint32_t *err) {
+  constexpr int kCols = BN < 32 ? 32 : BN;  // tensor-memory columns (power of two >= 32)
+  extern __shared__ __align__(1024) unsigned char smem_tc[];
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_tc) + 1023) & ~uintptr_t(1023));
+  unsigned char *sA = base;                  // 128 x 64 BF16 = 16 KB
+  unsigned char *sB = base + kTcBM * 128;    // BN x 64 BF16
+  uint64_t *bar_load = reinterpret_cast<uint64_t *>(sB + BN * 128);
+  uint64_t *bar_mma = bar_load + 1;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + 1);
+  int *flag = reinterpret_cast<int *>(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(bar_load, 1);
+    mbar_init(bar_mma, 1);
+    fence_barrier_init();
+    *flag = 1;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  const int m0 = blockIdx.y * kTcBM, n0 = blockIdx.x * BN;
+  const int kb = blockIdx.z * k_per_split, ke = min(K, kb + k_per_split);
+  const uint32_t idesc = idesc_bf16(BN);
+  uint32_t phase = 0;
+  bool pending = false;  // an MMA commit not yet waited for (thread 0)
+  for (int k0 = kb; k0 < ke; k0 += kTcBK) {
+    if (threadIdx.x == 0) {
+      mbar_arrive_expect_tx(bar_load, (uint32_t)(kTcBM * 128 + BN * 128));
+      tma_load_2d(sA, &tmA, k0, m0, bar_load);
+      tma_load_2d(sB, &tmB, k0, n0, bar_load);
+      bool ok = wait_bounded(bar_load, phase, err);
+      if (ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint64_t da = smem_desc_sw128(sA), db = smem_desc_sw128(sB);
+#pragma unroll
+        for (int j = 0; j < kTcBK / 16; j++)  // K = 16 per instruction: +32 bytes
+          umma_bf16(tmem, da + 2 * j, db + 2 * j, idesc, (k0 > kb || j > 0) ? 1u : 0u);
+        umma_commit(bar_mma);
+        pending = true;
+        // The commit completes when the MMAs have read the staging buffers
+        // and written the accumulator.
+        ok = wait_bounded(bar_mma, phase, err);
+        pending = !ok;
+      }
+      if (!ok) *flag = 0;
+    }
+    phase ^= 1u;
+    __syncthreads();
+    if (!*flag) break;
+  }
+  if (threadIdx.x == 0 && pending) wait_bounded(bar_mma, phase ^ 1u, err);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  if (*flag && kb < ke) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      if (BN >= 32)
+        tmem_load_32<32>(lane_base + (uint32_t)c0, v);
+      else
+        tmem_load_16(lane_base + (uint32_t)c0, v);
+      if (row < M) {
+        float *crow = C + (size_t)row * ldc;
+#pragma unroll
+        for (int i = 0; i < (BN >= 32 ? 32 : BN); i++) {
+          const int col = n0 + c0 + i;
+          if (col < N) {
+            if (mode == kGemmStore)
+              crow[col] = v[i];
+            else if (mode == kGemmAccumulate)
+              crow[col] += v[i];
+            else
+              atomicAdd(crow + col, v[i]);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols)
+                 : "memory");
+}
+
+// ---------------------------------------------------------------- host side
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 2-D map of a row-major BF16 matrix (rows x cols, leading dimension ld),
+// boxes of box_rows x 64 with 128-byte swizzle.
+bool make_map(CUtensorMap *map, const __nv_bfloat16 *ptr, int rows, int cols, int ld,
+              int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+  cuuint32_t estride[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(ptr), gdim,
+            gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Dynamic shared memory per CTA.  For BN = 128 it is padded to 56 KB so at
+// most 4 CTAs share an SM: 4 x 128 tensor-memory columns = the SM's 512, so
+// no tcgen05.alloc has to wait for another CTA to free its columns.
+template <int BN>
+constexpr size_t tc_smem() {
+  return BN >= 128 ? (size_t)56 * 1024 : 1024 + (size_t)kTcBM * 128 + (size_t)BN * 128 + 64;
+}
+
+}  // namespace
+
+cudaError_t launch_gemm_tn_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb,
+                              float *C, int ldc, int M, int N, int K, int mode, int splits,
+                              uint32_t *err, cudaStream_t s) {
+  if ((lda & 7) || (ldb & 7) || M <= 0 || K <= 0 || (N != 128 && N != 16))
+    return cudaErrorInvalidValue;
+  if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15)
+    return cudaErrorInvalidValue;
+  if (splits < 1) splits = 1;
+  int kps = (K + splits - 1) / splits;
+  kps = (kps + kTcBK - 1) / kTcBK * kTcBK;
+  splits = (K + kps - 1) / kps;
+  if (splits > 1) mode = kGemmAtomic;
+  CUtensorMap ta, tb;
+  if (!make_map(&ta, A, M, K, lda, kTcBM) || !make_map(&tb, B, N, K, ldb, N))
+    return cudaErrorInvalidValue;
+  dim3 grid(1, (M + kTcBM - 1) / kTcBM, splits);
+  if (N == 128) {
+    static bool configured = false;  // 56 KB is above the 48 KB default limit
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(k_gemm_tn_tc<128>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)tc_smem<128>());
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    k_gemm_tn_tc<128><<<grid, 128, tc_smem<128>(), s>>>(ta, tb, C, ldc, M, N, K, kps, mode, err);
+  } else {
+    k_gemm_tn_tc<16><<<grid, 128, tc_smem<16>(), s>>>(ta, tb, C, ldc, M, N, K, kps, mode, err);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace aco

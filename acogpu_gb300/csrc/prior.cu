@@ -43,6 +43,7 @@ struct aco_prior {
   float *dlogit = nullptr, *out = nullptr, *loss = nullptr, *scratch = nullptr;
   float *gW1full = nullptr;  // [128][16] gradient of the padded first layer
   int64_t step = 0;
+  int engine = ACO_GEMM_TCGEN05;  // enum aco_gemm_engine
   std::string err;
 };
 
@@ -66,10 +67,45 @@ cudaError_t alloc(T **p, size_t count) {
   return cudaMalloc(reinterpret_cast<void **>(p), count * sizeof(T) + 16);
 }
 
+// One MLP product on the selected tensor-core engine.
+cudaError_t gemm(aco_prior *p, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb,
+                 float *C, int ldc, int M, int N, int K, int mode, int splits) {
+  if (p->engine == ACO_GEMM_TCGEN05)
+    return launch_gemm_tn_tc(A, lda, B, ldb, C, ldc, M, N, K, mode, splits,
+                             reinterpret_cast<uint32_t *>(p->scratch + 2), p->stream);
+  return launch_gemm_tn(A, lda, B, ldb, C, ldc, M, N, K, mode, splits, p->stream);
+}
+
+// Every transfer of the prior goes through its own stream.  The stream is
+// non-blocking, so it is not ordered after the legacy stream that a plain
+// cudaMemcpy / cudaMemset uses, and a pageable upload may return before its
+// DMA has landed: a kernel launched next could read the old contents.
+cudaError_t copy_sync(aco_prior *p, void *dst, const void *src, size_t bytes,
+                      cudaMemcpyKind kind) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, p->stream);
+  return e == cudaSuccess ? cudaStreamSynchronize(p->stream) : e;
+}
+
+cudaError_t zero(aco_prior *p, void *dst, size_t bytes) {
+  return cudaMemsetAsync(dst, 0, bytes, p->stream);
+}
+
+// Reads (and clears) the device word the tensor-core GEMM sets when one of
+// its bounded waits ran out.
+int gemm_status(aco_prior *p) {
+  uint32_t h = 0;
+  uint32_t *w = reinterpret_cast<uint32_t *>(p->scratch + 2);
+  if (copy_sync(p, &h, w, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return pfail(p, ACO_ERR_CUDA, "read gemm status");
+  if (!h) return ACO_OK;
+  zero(p, w, 4);
+  return pfail(p, ACO_ERR_DEVICE_TIMEOUT, "tensor-core gemm wait timed out");
+}
+
 // Refreshes the BF16 copies of W1 (padded to 16 inputs) and W2 from the masters.
 int sync_bf16(aco_prior *p) {
   std::vector<float> w(kParamCount);
-  ACO_PCUDA(p, cudaMemcpy(w.data(), p->w, sizeof(float) * kParamCount, cudaMemcpyDeviceToHost),
+  ACO_PCUDA(p, copy_sync(p, w.data(), p->w, sizeof(float) * kParamCount, cudaMemcpyDeviceToHost),
             "read weights");
   std::vector<__nv_bfloat16> w1(kHidden * kFeatPad), w2(kHidden * kHidden), w2t(kHidden * kHidden);
   for (int o = 0; o < kHidden; o++)
@@ -81,9 +117,9 @@ int sync_bf16(aco_prior *p) {
       w2[o * kHidden + i] = __float2bfloat16_rn(w[kParamW2 + o * kHidden + i]);
       w2t[i * kHidden + o] = w2[o * kHidden + i];
     }
-  ACO_PCUDA(p, cudaMemcpy(p->w1b, w1.data(), w1.size() * 2, cudaMemcpyHostToDevice), "w1");
-  ACO_PCUDA(p, cudaMemcpy(p->w2b, w2.data(), w2.size() * 2, cudaMemcpyHostToDevice), "w2");
-  ACO_PCUDA(p, cudaMemcpy(p->w2tb, w2t.data(), w2t.size() * 2, cudaMemcpyHostToDevice), "w2t");
+  ACO_PCUDA(p, copy_sync(p, p->w1b, w1.data(), w1.size() * 2, cudaMemcpyHostToDevice), "w1");
+  ACO_PCUDA(p, copy_sync(p, p->w2b, w2.data(), w2.size() * 2, cudaMemcpyHostToDevice), "w2");
+  ACO_PCUDA(p, copy_sync(p, p->w2tb, w2t.data(), w2t.size() * 2, cudaMemcpyHostToDevice), "w2t");
   return ACO_OK;
 }
 
@@ -113,13 +149,13 @@ int forward_backward(aco_prior *p, const __nv_bfloat16 *X, const float *Y, int B
   cudaStream_t s = p->stream;
   const int splits = std::max(1, std::min(64, B / 1024));
   // Z1 = X W1^T ; H1 = relu(Z1 + b1)
-  ACO_PCUDA(p, launch_gemm_tn(X, kFeatPad, p->w1b, kFeatPad, p->Z, kHidden, B, kHidden, kFeatPad,
-                              kGemmStore, 1, s), "gemm z1");
+  ACO_PCUDA(p, gemm(p, X, kFeatPad, p->w1b, kFeatPad, p->Z, kHidden, B, kHidden, kFeatPad,
+                    kGemmStore, 1), "gemm z1");
   ACO_PCUDA(p, launch_bias_relu(p->Z, p->w + kParamB1, B, kHidden, p->H1,
                                 backward ? p->H1t : nullptr, B, s), "h1");
   // Z2 = H1 W2^T ; H2 = relu(Z2 + b2)
-  ACO_PCUDA(p, launch_gemm_tn(p->H1, kHidden, p->w2b, kHidden, p->Z, kHidden, B, kHidden, kHidden,
-                              kGemmStore, 1, s), "gemm z2");
+  ACO_PCUDA(p, gemm(p, p->H1, kHidden, p->w2b, kHidden, p->Z, kHidden, B, kHidden, kHidden,
+                    kGemmStore, 1), "gemm z2");
   ACO_PCUDA(p, launch_bias_relu(p->Z, p->w + kParamB2, B, kHidden, p->H2, nullptr, 0, s), "h2");
   if (!backward) {
     ACO_PCUDA(p, launch_head(p->H2, p->w + kParamW3, p->w + kParamB3, valid, nullptr, 1.0f, 1.0f,
@@ -133,27 +169,28 @@ int forward_backward(aco_prior *p, const __nv_bfloat16 *X, const float *Y, int B
   ACO_PCUDA(p, launch_grad_hidden2(p->dlogit, p->w + kParamW3, p->H2, B, p->dZ2, p->dZ2t, B,
                                    p->g + kParamB2, s), "dz2");
   // dW2 += dZ2^T H1
-  ACO_PCUDA(p, launch_gemm_tn(p->dZ2t, B, p->H1t, B, p->g + kParamW2, kHidden, kHidden, kHidden, B,
-                              kGemmAtomic, splits, s), "gemm dw2");
+  ACO_PCUDA(p, gemm(p, p->dZ2t, B, p->H1t, B, p->g + kParamW2, kHidden, kHidden, kHidden, B,
+                    kGemmAtomic, splits), "gemm dw2");
   // dH1 = dZ2 W2 ; dZ1 = dH1 * [H1 > 0]
-  ACO_PCUDA(p, launch_gemm_tn(p->dZ2, kHidden, p->w2tb, kHidden, p->Z, kHidden, B, kHidden, kHidden,
-                              kGemmStore, 1, s), "gemm dh1");
+  ACO_PCUDA(p, gemm(p, p->dZ2, kHidden, p->w2tb, kHidden, p->Z, kHidden, B, kHidden, kHidden,
+                    kGemmStore, 1), "gemm dh1");
   ACO_PCUDA(p, launch_grad_hidden1(p->Z, p->H1, B, p->dZ1t, B, p->g + kParamB1, s), "dz1");
   // dW1 += dZ1^T X
   ACO_PCUDA(p, launch_transpose_feats(X, B, p->Xt, B, s), "xt");
-  ACO_PCUDA(p, launch_gemm_tn(p->dZ1t, B, p->Xt, B, p->gW1full, kFeatPad, kHidden, kFeatPad, B,
-                              kGemmAtomic, splits, s), "gemm dw1");
+  ACO_PCUDA(p, gemm(p, p->dZ1t, B, p->Xt, B, p->gW1full, kFeatPad, kHidden, kFeatPad, B,
+                    kGemmAtomic, splits), "gemm dw1");
   return ACO_OK;
 }
 
 // Moves the padded first-layer gradient into the packed gradient vector.
+// Each thread owns one padded entry: it reads it, adds it (real features
+// only) and clears it, so no entry is cleared by another thread first.
 __global__ void k_pack_w1_grad(float *gW1full, float *g) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < kHidden * kFeatures) {
-    const int o = t / kFeatures, f = t % kFeatures;
-    g[kParamW1 + t] += gW1full[o * kFeatPad + f];
-  }
-  if (t < kHidden * kFeatPad) gW1full[t] = 0.0f;
+  if (t >= kHidden * kFeatPad) return;
+  const int o = t / kFeatPad, f = t % kFeatPad;
+  if (f < kFeatures) g[kParamW1 + o * kFeatures + f] += gW1full[t];
+  gW1full[t] = 0.0f;
 }
 
 int pack_grads(aco_prior *p) {
@@ -183,8 +220,8 @@ int upload_examples(aco_prior *p, const float *feats, const float *labels, int E
   }
   ACO_PCUDA(p, alloc(Xd, x.size()), "alloc");
   ACO_PCUDA(p, alloc(Yd, y.size()), "alloc");
-  ACO_PCUDA(p, cudaMemcpy(*Xd, x.data(), x.size() * 2, cudaMemcpyHostToDevice), "upload x");
-  ACO_PCUDA(p, cudaMemcpy(*Yd, y.data(), y.size() * 4, cudaMemcpyHostToDevice), "upload y");
+  ACO_PCUDA(p, copy_sync(p, *Xd, x.data(), x.size() * 2, cudaMemcpyHostToDevice), "upload x");
+  ACO_PCUDA(p, copy_sync(p, *Yd, y.data(), y.size() * 4, cudaMemcpyHostToDevice), "upload y");
   return ACO_OK;
 }
 
@@ -222,12 +259,14 @@ int aco_prior_create(uint64_t seed, aco_prior **out) {
   for (int t = 0; t < kHidden * kFeatures; t++) w[kParamW1 + t] = nd(rng) * sqrtf(2.0f / kFeatures);
   for (int t = 0; t < kHidden * kHidden; t++) w[kParamW2 + t] = nd(rng) * sqrtf(2.0f / kHidden);
   for (int t = 0; t < kHidden; t++) w[kParamW3 + t] = nd(rng) * sqrtf(1.0f / kHidden);
-  cudaMemcpy(p->w, w.data(), sizeof(float) * kParamCount, cudaMemcpyHostToDevice);
-  cudaMemset(p->g, 0, sizeof(float) * kParamCount);
-  cudaMemset(p->m1, 0, sizeof(float) * kParamCount);
-  cudaMemset(p->m2, 0, sizeof(float) * kParamCount);
-  cudaMemset(p->gW1full, 0, sizeof(float) * kHidden * kFeatPad);
-  if (sync_bf16(p) != ACO_OK) {
+  zero(p, p->g, sizeof(float) * kParamCount);
+  zero(p, p->m1, sizeof(float) * kParamCount);
+  zero(p, p->m2, sizeof(float) * kParamCount);
+  zero(p, p->gW1full, sizeof(float) * kHidden * kFeatPad);
+  zero(p, p->scratch, sizeof(float) * 4);
+  if (copy_sync(p, p->w, w.data(), sizeof(float) * kParamCount, cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      sync_bf16(p) != ACO_OK) {
     aco_prior_destroy(p);
     return ACO_ERR_CUDA;
   }
@@ -237,13 +276,15 @@ int aco_prior_create(uint64_t seed, aco_prior **out) {
 
 int aco_prior_get_weights(aco_prior *p, float *out) {
   if (!p || !out) return ACO_ERR_INVALID_ARGUMENT;
-  ACO_PCUDA(p, cudaMemcpy(out, p->w, sizeof(float) * kParamCount, cudaMemcpyDeviceToHost), "read");
+  ACO_PCUDA(p, copy_sync(p, out, p->w, sizeof(float) * kParamCount, cudaMemcpyDeviceToHost),
+            "read");
   return ACO_OK;
 }
 
 int aco_prior_set_weights(aco_prior *p, const float *in) {
   if (!p || !in) return ACO_ERR_INVALID_ARGUMENT;
-  ACO_PCUDA(p, cudaMemcpy(p->w, in, sizeof(float) * kParamCount, cudaMemcpyHostToDevice), "write");
+  ACO_PCUDA(p, copy_sync(p, p->w, in, sizeof(float) * kParamCount, cudaMemcpyHostToDevice),
+            "write");
   return sync_bf16(p);
 }
 
@@ -261,8 +302,9 @@ int aco_prior_add_examples(aco_prior *p, aco_colony *c) {
     ACO_PCUDA(p, alloc(&X, (size_t)cap * kFeatPad), "alloc examples");
     ACO_PCUDA(p, alloc(&Y, (size_t)cap), "alloc labels");
     if (p->E) {
-      ACO_PCUDA(p, cudaMemcpy(X, p->X, (size_t)p->E * kFeatPad * 2, cudaMemcpyDeviceToDevice), "copy");
-      ACO_PCUDA(p, cudaMemcpy(Y, p->Y, (size_t)p->E * 4, cudaMemcpyDeviceToDevice), "copy");
+      ACO_PCUDA(p, copy_sync(p, X, p->X, (size_t)p->E * kFeatPad * 2, cudaMemcpyDeviceToDevice),
+                "copy");
+      ACO_PCUDA(p, copy_sync(p, Y, p->Y, (size_t)p->E * 4, cudaMemcpyDeviceToDevice), "copy");
     }
     cudaFree(p->X);
     cudaFree(p->Y);
@@ -315,13 +357,13 @@ int aco_prior_train(aco_prior *p, int32_t epochs, int32_t batch, float lr, uint6
   if (tail < B) {  // the last batch is padded with label -1 rows
     ACO_PCUDA(p, alloc(&Xtail, (size_t)B * kFeatPad), "alloc");
     ACO_PCUDA(p, alloc(&Ytail, (size_t)B), "alloc");
-    ACO_PCUDA(p, cudaMemset(Xtail, 0, (size_t)B * kFeatPad * 2), "memset");
+    ACO_PCUDA(p, zero(p, Xtail, (size_t)B * kFeatPad * 2), "memset");
     std::vector<float> neg((size_t)B, -1.0f);
-    ACO_PCUDA(p, cudaMemcpy(Ytail, neg.data(), (size_t)B * 4, cudaMemcpyHostToDevice), "init");
-    ACO_PCUDA(p, cudaMemcpy(Xtail, p->X + (size_t)(nb - 1) * B * kFeatPad,
-                            (size_t)tail * kFeatPad * 2, cudaMemcpyDeviceToDevice), "tail");
-    ACO_PCUDA(p, cudaMemcpy(Ytail, p->Y + (size_t)(nb - 1) * B, (size_t)tail * 4,
-                            cudaMemcpyDeviceToDevice), "tail");
+    ACO_PCUDA(p, copy_sync(p, Ytail, neg.data(), (size_t)B * 4, cudaMemcpyHostToDevice), "init");
+    ACO_PCUDA(p, copy_sync(p, Xtail, p->X + (size_t)(nb - 1) * B * kFeatPad,
+                           (size_t)tail * kFeatPad * 2, cudaMemcpyDeviceToDevice), "tail");
+    ACO_PCUDA(p, copy_sync(p, Ytail, p->Y + (size_t)(nb - 1) * B, (size_t)tail * 4,
+                           cudaMemcpyDeviceToDevice), "tail");
   }
   float loss = 0.0f;
   for (int ep = 0; ep < epochs; ep++) {
@@ -347,7 +389,7 @@ int aco_prior_train(aco_prior *p, int32_t epochs, int32_t batch, float lr, uint6
   cudaFree(Xtail);
   cudaFree(Ytail);
   if (last_loss) *last_loss = loss;
-  return ACO_OK;
+  return gemm_status(p);
 }
 
 int aco_prior_loss_and_grads(aco_prior *p, const float *feats, const float *labels, int32_t E,
@@ -372,7 +414,7 @@ int aco_prior_loss_and_grads(aco_prior *p, const float *feats, const float *labe
   cudaFree(X);
   cudaFree(Y);
   if (loss) *loss = h;
-  return s;
+  return s ? s : gemm_status(p);
 }
 
 int aco_prior_predict(aco_prior *p, const float *feats, int32_t E, float *probs) {
@@ -389,7 +431,7 @@ int aco_prior_predict(aco_prior *p, const float *feats, int32_t E, float *probs)
   if (!s && cudaStreamSynchronize(p->stream) != cudaSuccess) s = ACO_ERR_CUDA;
   cudaFree(X);
   cudaFree(Y);
-  return s;
+  return s ? s : gemm_status(p);
 }
 
 int aco_prior_apply(aco_prior *p, aco_colony *c, float floor_) {
@@ -418,6 +460,7 @@ int aco_prior_apply(aco_prior *p, aco_colony *c, float floor_) {
   cudaFree(X);
   cudaFree(prob);
   if (s) return pfail(p, s, "apply failed");
+  if (int g = gemm_status(p)) return g;
   // The colony's candidate table changed: a captured iteration graph stays
   // valid (same buffers), the staged copy is reloaded at every launch.
   return ACO_OK;
@@ -439,13 +482,56 @@ int aco_colony_edge_features(aco_colony *c, float *out) {
     s = ACO_ERR_CUDA;
   if (!s) {
     std::vector<__nv_bfloat16> h((size_t)E * kFeatPad);
-    cudaMemcpy(h.data(), X, h.size() * 2, cudaMemcpyDeviceToHost);
-    for (int e = 0; e < E; e++)
+    if (cudaMemcpyAsync(h.data(), X, h.size() * 2, cudaMemcpyDeviceToHost, c->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+      s = ACO_ERR_CUDA;
+    for (int e = 0; e < (s ? 0 : E); e++)
       for (int f = 0; f < kFeatures; f++)
         out[(size_t)e * kFeatures + f] = __bfloat162float(h[(size_t)e * kFeatPad + f]);
   }
   cudaFree(X);
   cudaFree(scratch);
+  return s;
+}
+
+int aco_prior_set_engine(aco_prior *p, int32_t engine) {
+  if (!p || (engine != ACO_GEMM_MMA_SYNC && engine != ACO_GEMM_TCGEN05))
+    return ACO_ERR_INVALID_ARGUMENT;
+  p->engine = engine;
+  return ACO_OK;
+}
+
+int aco_gemm_bf16_tn(const uint16_t *A, const uint16_t *B, float *C, int32_t M, int32_t N,
+                     int32_t K, int32_t splits, int32_t engine) {
+  if (!A || !B || !C || M < 1 || N < 1 || K < 1 || (K & 7)) return ACO_ERR_INVALID_ARGUMENT;
+  if (engine == ACO_GEMM_TCGEN05 && N != 128 && N != 16) return ACO_ERR_UNSUPPORTED;
+  __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+  float *dC = nullptr;
+  uint32_t *derr = nullptr;
+  int s = ACO_OK;
+  if (alloc(&dA, (size_t)M * K) != cudaSuccess || alloc(&dB, (size_t)N * K) != cudaSuccess ||
+      alloc(&dC, (size_t)M * N) != cudaSuccess || alloc(&derr, 1) != cudaSuccess)
+    s = ACO_ERR_OUT_OF_MEMORY;
+  if (!s) {
+    cudaMemcpy(dA, A, (size_t)M * K * 2, cudaMemcpyHostToDevice);
+    cudaMemcpy(dB, B, (size_t)N * K * 2, cudaMemcpyHostToDevice);
+    cudaMemset(dC, 0, (size_t)M * N * 4);
+    cudaMemset(derr, 0, 4);
+    cudaError_t e = engine == ACO_GEMM_TCGEN05
+                        ? launch_gemm_tn_tc(dA, K, dB, K, dC, N, M, N, K, kGemmStore, splits,
+                                            derr, 0)
+                        : launch_gemm_tn(dA, K, dB, K, dC, N, M, N, K, kGemmStore, splits, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    uint32_t herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(C, dC, (size_t)M * N * 4, cudaMemcpyDeviceToHost);
+    s = e != cudaSuccess ? ACO_ERR_CUDA : (herr ? ACO_ERR_DEVICE_TIMEOUT : ACO_OK);
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  cudaFree(derr);
   return s;
 }
 

@@ -56,6 +56,7 @@ def _setup(L):
     L.aco_prior_last_error.restype = ctypes.c_char_p
     L.aco_prior_destroy.argtypes = [_vp]
     L.aco_prior_destroy.restype = None
+    L.aco_prior_set_engine.argtypes = [_vp, ctypes.c_int32]
     L.aco_colony_edge_features.argtypes = [_vp, _f32p]
     L.aco_colony_read_candidate_heuristic.argtypes = [_vp, _f32p]
     L._prior_ready = True
@@ -84,7 +85,10 @@ def candidate_heuristic(colony: Colony):
 
 
 class EdgePrior:
-    def __init__(self, seed=0):
+    """engine: ACO_GEMM_TCGEN05 (default; TMA + TMEM tensor cores) or
+    ACO_GEMM_MMA_SYNC (warp-level mma.sync) for the MLP's products."""
+
+    def __init__(self, seed=0, engine=None):
         self._L = lib()
         _setup(self._L)
         self._h = None
@@ -93,6 +97,11 @@ class EdgePrior:
         if st:
             raise AcoError(st, "aco_prior_create")
         self._h = h
+        if engine is not None:
+            self.set_engine(engine)
+
+    def set_engine(self, engine):
+        self._check(self._L.aco_prior_set_engine(self._h, int(engine)), "set_engine")
 
     def _check(self, st, what):
         if st:

@@ -456,7 +456,7 @@ def run_learned(args, rank, world, local):
     """Learned prior vs plain ACO at equal GPU time (scaled-down C5)."""
     import torch
     import acogpu_gb300 as aco
-    from acogpu_gb300 import instances
+    from acogpu_gb300 import _abi, instances
     from acogpu_gb300.prior import EdgePrior
     torch.cuda.set_device(local)
     g = instances.SplitMix64(31)
@@ -478,6 +478,17 @@ def run_learned(args, rank, world, local):
     loss0 = prior.train(epochs=1, batch=65536, lr=2e-3, seed=1)
     loss = prior.train(epochs=args.epochs, batch=65536, lr=1e-3, seed=2)
     train_s = time.perf_counter() - t0
+    # One more epoch on each GEMM engine, timed alone; the trained weights are
+    # put back afterwards so the evaluation below is unaffected.
+    w_trained = prior.weights()
+    epoch_s = {}
+    for name, eng in (("tcgen05", _abi.ACO_GEMM_TCGEN05), ("mma_sync", _abi.ACO_GEMM_MMA_SYNC)):
+        prior.set_engine(eng)
+        t1 = time.perf_counter()
+        prior.train(epochs=1, batch=65536, lr=1e-6, seed=3)
+        epoch_s[name] = time.perf_counter() - t1
+    prior.set_engine(_abi.ACO_GEMM_TCGEN05)
+    prior.set_weights(w_trained)
 
     sizes = instances.batch_sizes(args.eval_instances, lo=200, hi=2000, seed=41)
     evals = [instances.uniform_instance(int(n), seed=30_000 + i) if i % 2 == 0 else
@@ -529,7 +540,8 @@ def run_learned(args, rank, world, local):
                         "inference_s": t_infer, "mean_best": best_learned,
                         "reaches_plain_within_0.1pct_at_s": reach},
             "training": {"examples": examples, "positives": positives, "loss_first_epoch": loss0,
-                         "loss_last_epoch": loss, "wall_s": train_s}}
+                         "loss_last_epoch": loss, "wall_s": train_s,
+                         "epoch_s_by_gemm_engine": epoch_s}}
 
 
 def main():

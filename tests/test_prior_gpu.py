@@ -54,28 +54,37 @@ def test_edge_features_match_numpy():
     assert np.allclose(f, ref, rtol=1e-2, atol=1e-3)
 
 
-def test_gradients_match_cpu_oracle():
+ENGINES = pytest.mark.parametrize("engine", [_abi.ACO_GEMM_TCGEN05, _abi.ACO_GEMM_MMA_SYNC],
+                                  ids=["tcgen05", "mma_sync"])
+
+
+@ENGINES
+def test_gradients_match_cpu_oracle(engine):
     """Loss and every parameter gradient of the GPU forward/backward kernels
     against the FP64 oracle (same BF16 rounding points)."""
     c, _, _, _ = colony(80, 9)
     X = edge_features(c)
     rng = np.random.default_rng(1)
     y = (rng.random(len(X)) < 0.2).astype(np.float32)
-    pr = EdgePrior(seed=7)
+    pr = EdgePrior(seed=7, engine=engine)
     w = pr.weights()
-    loss, g = pr.loss_and_grads(X, y, pos_weight=3.0)
     lref, gref = mo.loss_and_grads(w, X, y, pos_weight=3.0)
-    assert abs(loss - lref) <= 2e-3 * abs(lref)
-    gp, rp = mo.unpack(g), mo.unpack(gref)
-    for name in ("W1", "b1", "W2", "b2", "w3", "b3"):
-        err = np.linalg.norm(gp[name] - rp[name]) / max(1e-12, np.linalg.norm(rp[name]))
-        assert err < 1e-2, (name, err)
+    rp = mo.unpack(gref)
+    # repeated: a race in the gradient reduction shows up as a run-to-run change
+    for rep in range(4):
+        loss, g = pr.loss_and_grads(X, y, pos_weight=3.0)
+        assert abs(loss - lref) <= 2e-3 * abs(lref)
+        gp = mo.unpack(g)
+        for name in ("W1", "b1", "W2", "b2", "w3", "b3"):
+            err = np.linalg.norm(gp[name] - rp[name]) / max(1e-12, np.linalg.norm(rp[name]))
+            assert err < 1e-2, (rep, name, err)
 
 
-def test_predict_matches_cpu_oracle():
+@ENGINES
+def test_predict_matches_cpu_oracle(engine):
     c, _, _, _ = colony(70, 4)
     X = edge_features(c)
-    pr = EdgePrior(seed=3)
+    pr = EdgePrior(seed=3, engine=engine)
     p = pr.predict(X)
     ref = mo.predict(pr.weights(), X)
     assert np.max(np.abs(p - ref)) < 5e-3
