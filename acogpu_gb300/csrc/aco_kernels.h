@@ -36,7 +36,9 @@ size_t construct_smem_bytes(int n, int K, int ants_per_block);
 cudaError_t configure_construct(size_t smem);
 cudaError_t configure_pheromone_rows(int ld);
 cudaError_t launch_construct(const ColonyDev &c, int ants_per_block, cudaStream_t s);
-// Candidate table staged in shared memory (k <= 32, n < 32768).
+// Candidate table staged in shared memory (k <= 32, n <= 2048); at most
+// kStagedMaxWarps warps (ants in flight) per CTA.
+constexpr int kStagedMaxWarps = 16;
 size_t construct_staged_smem_bytes(int n, int ld, bool aging, int warps);
 cudaError_t configure_construct_staged(size_t smem);
 cudaError_t launch_construct_staged(const ColonyDev &c, const int16_t *nn16, int grid, int warps,

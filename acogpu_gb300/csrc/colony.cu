@@ -213,7 +213,7 @@ int plan_construction(aco_colony *c) {
     return ACO_OK;
   const int sms = c->num_sms > 0 ? c->num_sms : 1;
   int warps = (c->m + sms - 1) / sms;
-  warps = warps < 1 ? 1 : (warps > 32 ? 32 : warps);
+  warps = warps < 1 ? 1 : (warps > kStagedMaxWarps ? kStagedMaxWarps : warps);
   const size_t smem = construct_staged_smem_bytes(c->n, c->ld, c->p.aging != 0, warps);
   if (smem > (size_t)c->max_smem_optin) {
     if (c->p.construct_mode == ACO_CONSTRUCT_STAGED)

@@ -349,7 +349,9 @@ __device__ __forceinline__ void reg_mark(uint32_t (&tw)[TW], int city, int lane)
   }
 }
 
-// Largest choice value among unvisited cities (register tabu version).
+// Largest choice value among unvisited cities (register tabu version).  The
+// plain rule issues the row loads four 128-city chunks at a time, so a scan
+// of n cities waits for ceil(n / 512) L2 round trips, not one per chunk.
 template <int TW>
 __device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&tw)[TW],
                                  const AntCtx &a, int lane) {
@@ -358,34 +360,57 @@ __device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&t
   const float *crow = c.choice + (size_t)cur * c.ld;
   const float *trow = c.tau + (size_t)cur * c.ld;
   const float *erow = c.eta + (size_t)cur * c.ld;
-  for (int base = 0; base < c.n; base += 128) {
-    const int j4 = base + lane * 4;
-    const int word = j4 >> 5;  // warp-uniform source per lane group
-    uint32_t v = __shfl_sync(kFull, tw[0], word & 31);
-    if (TW > 1) {
-      const uint32_t v1 = __shfl_sync(kFull, tw[TW > 1 ? 1 : 0], word & 31);
-      v = (word >> 5) ? v1 : v;
+  if (!a.blend) {
+#pragma unroll
+    for (int t0 = 0; t0 < 8 * TW; t0 += 4) {  // n <= 1024 * TW
+      if (t0 * 128 >= c.n) break;
+      float4 q[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const int j4 = (t0 + t) * 128 + lane * 4;  // j4 < n implies j4 + 3 < ld (ld % 32 == 0)
+        q[t] = j4 < c.n ? __ldcg(reinterpret_cast<const float4 *>(crow + j4))
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const int j4 = (t0 + t) * 128 + lane * 4;
+        const uint32_t v =
+            __shfl_sync(kFull, tw[(t0 + t) >> 3], ((t0 + t) * 4 + (lane >> 3)) & 31);
+        const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
+        const float qq[4] = {q[t].x, q[t].y, q[t].z, q[t].w};
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          if (!((bits >> r) & 1u) && j4 + r < c.n && qq[r] > bw) {
+            bw = qq[r];
+            bj = j4 + r;
+          }
+        }
+      }
     }
-    if (j4 >= c.n) continue;
-    const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
-    if (bits == 0xfu) continue;
-    float q[4];
-    if (!a.blend) {
-      const float4 t = *reinterpret_cast<const float4 *>(crow + j4);
-      q[0] = t.x; q[1] = t.y; q[2] = t.z; q[3] = t.w;
-    } else {
+  } else {  // aging blend (young ants after convergence): tau and eta rows
+    for (int base = 0; base < c.n; base += 128) {
+      const int j4 = base + lane * 4;
+      const int word = j4 >> 5;  // warp-uniform source per lane group
+      uint32_t v = __shfl_sync(kFull, tw[0], word & 31);
+      if (TW > 1) {
+        const uint32_t v1 = __shfl_sync(kFull, tw[TW > 1 ? 1 : 0], word & 31);
+        v = (word >> 5) ? v1 : v;
+      }
+      if (j4 >= c.n) continue;
+      const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
+      if (bits == 0xfu) continue;
       const float4 t = *reinterpret_cast<const float4 *>(trow + j4);
       const float4 e = *reinterpret_cast<const float4 *>(erow + j4);
-      q[0] = blend_fitness(t.x, e.x, a.meanc, a.ratio, c.use_alpha, c.alpha);
-      q[1] = blend_fitness(t.y, e.y, a.meanc, a.ratio, c.use_alpha, c.alpha);
-      q[2] = blend_fitness(t.z, e.z, a.meanc, a.ratio, c.use_alpha, c.alpha);
-      q[3] = blend_fitness(t.w, e.w, a.meanc, a.ratio, c.use_alpha, c.alpha);
-    }
+      const float q[4] = {blend_fitness(t.x, e.x, a.meanc, a.ratio, c.use_alpha, c.alpha),
+                          blend_fitness(t.y, e.y, a.meanc, a.ratio, c.use_alpha, c.alpha),
+                          blend_fitness(t.z, e.z, a.meanc, a.ratio, c.use_alpha, c.alpha),
+                          blend_fitness(t.w, e.w, a.meanc, a.ratio, c.use_alpha, c.alpha)};
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-      if (!((bits >> r) & 1u) && j4 + r < c.n && q[r] > bw) {
-        bw = q[r];
-        bj = j4 + r;
+      for (int r = 0; r < 4; r++) {
+        if (!((bits >> r) & 1u) && j4 + r < c.n && q[r] > bw) {
+          bw = q[r];
+          bj = j4 + r;
+        }
       }
     }
   }
@@ -404,6 +429,26 @@ __device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&t
 // ant's whole tour) is a template parameter so the loop carries no per-step
 // test of it.  Rows of the staged table are padded to 32 entries with id -1
 // and weight 0, so every lane loads unconditionally.
+//
+// One step, with no data-dependent branch on the common path:
+//  * lane r holds candidate r: its id and its weight, zeroed when the city is
+//    visited (one __shfl_sync of the owner's tabu word);
+//  * the 32 weights go through a per-warp shared buffer and every lane reads
+//    all of them back with broadcast 16-byte loads;
+//  * lane l forms the reference's sequential prefix s_l = (..(w_0 + w_1) +
+//    ..) + w_l as acc = fma(w_e, incl_e, acc) over e = 0..31 with incl_e = 1
+//    for e <= l and 0 after: w*1 + acc rounds exactly like the reference's
+//    float add, and w*0 + acc = acc, so every lane runs the same 32 FMAs and
+//    lane 31 ends with the full sum S (zero weights change no non-negative
+//    float sum, as in the reference, which adds them too);
+//  * the pick is the first candidate with !(s <= u*S) (src/Colony.cu:833-846):
+//    prefixes never decrease, so the crossing lanes form a suffix of the warp
+//    and the first of them is a ballot + ffs; the crossing candidate always
+//    has a non-zero weight.  No crossing (S = 0, or u*S rounding up to S)
+//    takes the fallback, as the reference does.
+// The uniforms of 32 consecutive steps are computed one per lane and
+// broadcast; the tour positions of the current 32-step block stay in one
+// register per lane and are stored together.
 template <int TW, bool BLEND>
 __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t akey, int start,
                                             uint32_t (&tw)[TW], float *wbuf, const int16_t *sids,
@@ -411,74 +456,69 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
                                             int lane, int64_t &fallbacks) {
   const int n = c.n;
   int32_t *trow = c.tours + (size_t)k * c.ld;
-  const unsigned lt = (1u << lane) - 1u;
   const float4 *wbuf4 = reinterpret_cast<const float4 *>(wbuf);
+  float incl[32];
+#pragma unroll
+  for (int e = 0; e < 32; e++) incl[e] = e <= lane ? 1.0f : 0.0f;
   int cur = start;
-  for (int x = 1; x < n; x++) {
-    const float u = aco_uniform_key(akey, (uint32_t)x);
-    const int id = sids[cur * 32 + lane];
-    float w;
-    if (!BLEND) {
-      w = scw[cur * 32 + lane];
-    } else {
-      a.meanc = smean[cur];  // every lane: the fallback scan uses it too
-      const size_t off = (size_t)cur * c.ldk + lane;
-      w = lane < c.K ? blend_fitness(c.tau_nn[off], __ldg(c.eta_nn + off), a.meanc, a.ratio,
-                                     c.use_alpha, c.alpha)
-                     : 0.0f;
-    }
-    // reg_visited shuffles with the full mask: every lane must call it.
-    const bool vis = reg_visited(tw, id < 0 ? 0 : id);
-    const bool unvisited = id >= 0 && !vis;
-    if (!unvisited) w = 0.0f;
-    const unsigned nz = __ballot_sync(kFull, w != 0.0f);
-    const int cnt = __popc(nz);
-    int next = -1;
-    if (cnt > 0) {
-      const bool mine_nz = w != 0.0f;
-      const int rank = __popc(nz & lt);
-      wbuf[mine_nz ? rank : cnt + __popc(~nz & lt)] = w;
+  bool ok = true;
+  for (int xb = 0; xb < n && ok; xb += 32) {
+    const float ublk = aco_uniform_key(akey, (uint32_t)(xb + lane));
+    int tpos = (xb == 0 && lane == 0) ? start : 0;  // tour position xb + lane
+    const int xe = min(n, xb + 32);
+#pragma unroll 1
+    for (int x = xb == 0 ? 1 : xb; x < xe; x++) {
+      const float u = __shfl_sync(kFull, ublk, x & 31);
+      const int id = sids[cur * 32 + lane];
+      float w;
+      if (!BLEND) {
+        w = scw[cur * 32 + lane];
+      } else {
+        a.meanc = smean[cur];  // every lane: the fallback scan uses it too
+        const size_t off = (size_t)cur * c.ldk + lane;
+        w = lane < c.K ? blend_fitness(c.tau_nn[off], __ldg(c.eta_nn + off), a.meanc, a.ratio,
+                                       c.use_alpha, c.alpha)
+                       : 0.0f;
+      }
+      // Padding entries (id -1) carry weight 0, so their tabu lookup result
+      // is irrelevant; every lane must take part in the shuffle.
+      const bool vis = reg_visited(tw, id & 0xffff);
+      if (vis) w = 0.0f;
+      wbuf[lane] = w;
       __syncwarp();
-      float s = 0.0f, mine = 0.0f;
+      float acc = 0.0f;
 #pragma unroll
-      for (int g = 0; g < 4; g++) {
-        if (g * 8 < cnt) {
-          const float4 p0 = wbuf4[2 * g], p1 = wbuf4[2 * g + 1];
-          const float v[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
-#pragma unroll
-          for (int e = 0; e < 8; e++) {
-            s = __fadd_rn(s, v[e]);
-            mine = (rank == g * 8 + e) ? s : mine;
-          }
+      for (int g = 0; g < 8; g++) {
+        const float4 p = wbuf4[g];
+        acc = __fmaf_rn(p.x, incl[4 * g + 0], acc);
+        acc = __fmaf_rn(p.y, incl[4 * g + 1], acc);
+        acc = __fmaf_rn(p.z, incl[4 * g + 2], acc);
+        acc = __fmaf_rn(p.w, incl[4 * g + 3], acc);
+      }
+      const float rnd = __fmul_rn(u, __shfl_sync(kFull, acc, 31));
+      const unsigned hit = __ballot_sync(kFull, !(acc <= rnd));
+      int next = __shfl_sync(kFull, id, (__ffs(hit) - 1) & 31);
+      if (hit == 0u || (unsigned)next >= (unsigned)n) {
+        if (hit != 0u) {  // a candidate id outside the instance: recorded, not used
+          ok = false;
+        } else if (c.fallback == ACO_FALLBACK_BEST) {
+          next = fallback_best_reg(c, cur, tw, a, lane);
+        } else {  // select_local_best on a full row of at most 32 cities (k == n)
+          const unsigned um = __ballot_sync(kFull, id >= 0 && !vis);
+          next = um ? __shfl_sync(kFull, id, 31 - __clz(um)) : -1;
+        }
+        fallbacks += hit == 0u;
+        if (next < 0 || next >= n) ok = false;  // no unvisited city, or a bad id
+        if (!ok) {
+          if (lane == 0) atomicOr(&c.st->error, kErrCheck);
+          break;
         }
       }
-      __syncwarp();
-      const float rnd = __fmul_rn(u, s);
-      const unsigned hit = __ballot_sync(kFull, mine_nz && !(mine <= rnd));
-      if (hit) next = __shfl_sync(kFull, id, __ffs(hit) - 1);
-      if (next >= n) {  // a candidate id outside the instance: recorded, not used
-        if (lane == 0) atomicOr(&c.st->error, kErrCheck);
-        return cur;
-      }
+      reg_mark(tw, next, lane);
+      tpos = lane == (x & 31) ? next : tpos;
+      cur = next;
     }
-    if (next < 0) {
-      if (c.fallback == ACO_FALLBACK_BEST) {
-        next = fallback_best_reg(c, cur, tw, a, lane);
-      } else {  // select_local_best on a full row of at most 32 cities (k == n)
-        const unsigned um = __ballot_sync(kFull, unvisited);
-        next = um ? __shfl_sync(kFull, id, 31 - __clz(um)) : -1;
-      }
-      fallbacks++;
-      if (next < 0 || next >= n) {  // no unvisited city (or a rule that needs a full row)
-        if (lane == 0) atomicOr(&c.st->error, kErrCheck);
-        return cur;
-      }
-    }
-    reg_mark(tw, next, lane);
-    if (lane == 0) trow[x] = next;
-    if (lane == 1) c.succT[(size_t)cur * c.ldm + k] = next;
-    if (lane == 2) c.predT[(size_t)next * c.ldm + k] = cur;
-    cur = next;
+    if (xb + lane < xe) trow[xb + lane] = tpos;
   }
   return cur;
 }
@@ -519,25 +559,26 @@ __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, f
     start = n - 1;
   }
   reg_mark(tw, start, lane);
-  if (lane == 0) trow[0] = start;
 
   int64_t fallbacks = 0;
-  const int last = (AGING && a.blend)
-                       ? staged_steps<TW, true>(c, k, akey, start, tw, wbuf, sids, scw, smean, a,
-                                                lane, fallbacks)
-                       : staged_steps<TW, false>(c, k, akey, start, tw, wbuf, sids, scw, smean, a,
-                                                 lane, fallbacks);
-  if (lane == 1) c.succT[(size_t)last * c.ldm + k] = start;
-  if (lane == 2) c.predT[(size_t)start * c.ldm + k] = last;
+  if (AGING && a.blend)
+    staged_steps<TW, true>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
+  else
+    staged_steps<TW, false>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
   __syncwarp();
+  // Tour length (order-free integer sum) and the transposed successor /
+  // predecessor of every city for the row-owned deposit, one edge per lane.
   int64_t len = 0;
   for (int i = lane; i < n; i += 32) {
     const int a0 = trow[i];
     const int b0 = trow[i + 1 == n ? 0 : i + 1];
-    if ((unsigned)a0 < (unsigned)n && (unsigned)b0 < (unsigned)n)
+    if ((unsigned)a0 < (unsigned)n && (unsigned)b0 < (unsigned)n) {
       len += c.dist[(size_t)a0 * c.ld + b0];
-    else
+      c.succT[(size_t)a0 * c.ldm + k] = b0;
+      c.predT[(size_t)b0 * c.ldm + k] = a0;
+    } else {
       atomicOr(&c.st->error, kErrCheck);
+    }
   }
   for (int o = 16; o; o >>= 1) len += __shfl_xor_sync(kFull, len, o);
   if (lane == 0) {
@@ -569,7 +610,8 @@ __host__ __device__ inline size_t staged_table_bytes(int n, int ld, bool aging) 
 }
 
 template <bool AGING, int TW>
-__global__ void __launch_bounds__(1024) k_construct_staged(ColonyDev c, const int16_t *nn16) {
+__global__ void __launch_bounds__(kStagedMaxWarps * 32)
+    k_construct_staged(ColonyDev c, const int16_t *nn16) {
   extern __shared__ __align__(128) unsigned char smem_staged[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
   const int n = c.n;
