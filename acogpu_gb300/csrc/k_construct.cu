@@ -438,17 +438,18 @@ __device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&t
 //  * lane l forms the reference's sequential prefix s_l = (..(w_0 + w_1) +
 //    ..) + w_l as acc = fma(w_e, incl_e, acc) over e = 0..31 with incl_e = 1
 //    for e <= l and 0 after: w*1 + acc rounds exactly like the reference's
-//    float add, and w*0 + acc = acc, so every lane runs the same 32 FMAs and
-//    lane 31 ends with the full sum S (zero weights change no non-negative
-//    float sum, as in the reference, which adds them too);
+//    float add, and w*0 + acc = acc, so every lane runs the same 32 FMAs
+//    (zero weights change no non-negative float sum, as in the reference,
+//    which adds them too); each lane also adds all 32 for the full sum S;
 //  * the pick is the first candidate with !(s <= u*S) (src/Colony.cu:833-846):
 //    prefixes never decrease, so the crossing lanes form a suffix of the warp
 //    and the first of them is a ballot + ffs; the crossing candidate always
 //    has a non-zero weight.  No crossing (S = 0, or u*S rounding up to S)
 //    takes the fallback, as the reference does.
-// The uniforms of 32 consecutive steps are computed one per lane and
-// broadcast; the tour positions of the current 32-step block stay in one
-// register per lane and are stored together.
+// The next row is loaded before the (rare) fallback test resolves.  The
+// uniforms of 32 consecutive steps are computed one per lane and broadcast;
+// the tour positions of the current 32-step block stay in one register per
+// lane and are stored together.
 template <int TW, bool BLEND>
 __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t akey, int start,
                                             uint32_t (&tw)[TW], float *wbuf, const int16_t *sids,
@@ -461,6 +462,8 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
 #pragma unroll
   for (int e = 0; e < 32; e++) incl[e] = e <= lane ? 1.0f : 0.0f;
   int cur = start;
+  int id = sids[cur * 32 + lane];
+  float wraw = BLEND ? 0.0f : scw[cur * 32 + lane];
   bool ok = true;
   for (int xb = 0; xb < n && ok; xb += 32) {
     const float ublk = aco_uniform_key(akey, (uint32_t)(xb + lane));
@@ -469,11 +472,8 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
 #pragma unroll 1
     for (int x = xb == 0 ? 1 : xb; x < xe; x++) {
       const float u = __shfl_sync(kFull, ublk, x & 31);
-      const int id = sids[cur * 32 + lane];
-      float w;
-      if (!BLEND) {
-        w = scw[cur * 32 + lane];
-      } else {
+      float w = wraw;
+      if (BLEND) {
         a.meanc = smean[cur];  // every lane: the fallback scan uses it too
         const size_t off = (size_t)cur * c.ldk + lane;
         w = lane < c.K ? blend_fitness(c.tau_nn[off], __ldg(c.eta_nn + off), a.meanc, a.ratio,
@@ -486,18 +486,30 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
       if (vis) w = 0.0f;
       wbuf[lane] = w;
       __syncwarp();
-      float acc = 0.0f;
+      // Two independent chains: this lane's prefix and the full sum S (the
+      // second fills the first's latency gaps and saves a broadcast).
+      float acc = 0.0f, sum = 0.0f;
 #pragma unroll
       for (int g = 0; g < 8; g++) {
         const float4 p = wbuf4[g];
         acc = __fmaf_rn(p.x, incl[4 * g + 0], acc);
+        sum = __fadd_rn(sum, p.x);
         acc = __fmaf_rn(p.y, incl[4 * g + 1], acc);
+        sum = __fadd_rn(sum, p.y);
         acc = __fmaf_rn(p.z, incl[4 * g + 2], acc);
+        sum = __fadd_rn(sum, p.z);
         acc = __fmaf_rn(p.w, incl[4 * g + 3], acc);
+        sum = __fadd_rn(sum, p.w);
       }
-      const float rnd = __fmul_rn(u, __shfl_sync(kFull, acc, 31));
+      const float rnd = __fmul_rn(u, sum);
       const unsigned hit = __ballot_sync(kFull, !(acc <= rnd));
       int next = __shfl_sync(kFull, id, (__ffs(hit) - 1) & 31);
+      // The next row, loaded before the fallback test resolves (an in-range
+      // stand-in keeps the loads inside the table) and reloaded if the
+      // fallback picks the city.
+      const int nx = (unsigned)next < (unsigned)n ? next : 0;
+      int id_next = sids[nx * 32 + lane];
+      float w_next = BLEND ? 0.0f : scw[nx * 32 + lane];
       if (hit == 0u || (unsigned)next >= (unsigned)n) {
         if (hit != 0u) {  // a candidate id outside the instance: recorded, not used
           ok = false;
@@ -513,10 +525,14 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
           if (lane == 0) atomicOr(&c.st->error, kErrCheck);
           break;
         }
+        id_next = sids[next * 32 + lane];
+        w_next = BLEND ? 0.0f : scw[next * 32 + lane];
       }
       reg_mark(tw, next, lane);
       tpos = lane == (x & 31) ? next : tpos;
       cur = next;
+      id = id_next;
+      wraw = w_next;
     }
     if (xb + lane < xe) trow[xb + lane] = tpos;
   }
