@@ -81,7 +81,8 @@ class AcoTuning(ctypes.Structure):
         ("row_threads", ctypes.c_int32),
         ("construct_ms", ctypes.c_float),
         ("rows_ms", ctypes.c_float),
-        ("reserved", ctypes.c_int32 * 4),
+        ("staged_instances", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
 

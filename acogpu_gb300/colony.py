@@ -442,7 +442,8 @@ class Batch:
         t = _abi.AcoTuning()
         self._check(self._L.aco_batch_autotune(self._h, ctypes.byref(t)), "batch autotune")
         return {"ants_per_block": t.ants_per_block, "row_threads": t.row_threads,
-                "construct_ms": t.construct_ms, "rows_ms": t.rows_ms}
+                "construct_ms": t.construct_ms, "rows_ms": t.rows_ms,
+                "staged_instances": t.staged_instances}
 
     def set_tuning(self, ants_per_block, row_threads=0):
         self._check(self._L.aco_batch_set_tuning(self._h, int(ants_per_block), int(row_threads)),

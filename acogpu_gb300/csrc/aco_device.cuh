@@ -60,6 +60,7 @@ struct ColonyDev {
   float *tau;
   float *choice;
   const int32_t *nn;
+  const int16_t *nn16;  // n x 32 candidate ids (-1 padded) when k <= 32, else null
   const float *eta_nn;
   float *tau_nn;
   float *choice_nn;

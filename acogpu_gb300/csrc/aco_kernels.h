@@ -39,7 +39,25 @@ cudaError_t launch_construct(const ColonyDev &c, int ants_per_block, cudaStream_
 // Candidate table staged in shared memory (k <= 32, n <= 2048); at most
 // kStagedMaxWarps warps (ants in flight) per CTA.
 constexpr int kStagedMaxWarps = 16;
-size_t construct_staged_smem_bytes(int n, int ld, bool aging, int warps);
+// Pitch of the candidate rows (nn, eta_nn, tau_nn, choice_nn, nn16) for
+// k <= 32: the staged step folds pitch/4 groups of four weights, and the
+// pitch takes one of four values so the fold length is a template constant.
+__host__ __device__ constexpr int staged_pitch(int K) {
+  return K <= 16 ? 16 : K <= 20 ? 20 : K <= 24 ? 24 : 32;
+}
+// Shared-memory layout of a staged table of n rows with pitch sp:
+//   [choice n*sp f32][ids n*sp int16, padded to 16 B][row means ld f32, aging]
+struct StagedLayout {
+  size_t ids_off, mean_off, table;
+};
+__host__ __device__ inline StagedLayout staged_layout(int n, int ld, int sp, bool aging) {
+  StagedLayout L;
+  L.ids_off = (size_t)n * sp * 4;
+  L.mean_off = L.ids_off + ((size_t)n * sp * 2 + 15) / 16 * 16;
+  L.table = L.mean_off + (aging ? (size_t)ld * 4 : 0);
+  return L;
+}
+size_t construct_staged_smem_bytes(int n, int ld, int sp, bool aging, int warps);
 cudaError_t configure_construct_staged(size_t smem);
 cudaError_t launch_construct_staged(const ColonyDev &c, const int16_t *nn16, int grid, int warps,
                                     cudaStream_t s);
@@ -51,13 +69,18 @@ cudaError_t launch_batch_epilogue(const ColonyDev *descs, int count, cudaStream_
 cudaError_t launch_batch_pheromone_rows(const ColonyDev *descs, const int2 *rowmap, int rows,
                                         int max_ld, bool deposit_and_evaporate, cudaStream_t s,
                                         int threads = 0);
-// Persistent construction over a queue of work items (instance, first ant, ants).
-size_t batch_construct_smem_bytes(int max_n, int max_k, int warps);
+// Persistent construction over a queue of work items (instance, first ant,
+// ants, staged).  The shared region holds a staged item's candidate table or
+// the per-warp tabu lists of an L2-row item.
+size_t batch_staged_table_bytes(int n, int ld, int sp, bool aging);
+size_t batch_region_bytes(int max_n, int max_k, int warps, size_t max_table);
+size_t batch_construct_smem_bytes(size_t region_bytes, int warps);
 cudaError_t configure_batch_construct(size_t smem);
-int batch_construct_blocks_per_sm(int warps, size_t smem, bool multi, bool aging);
+int batch_construct_blocks_per_sm(int warps, size_t smem, bool multi, int sp, bool aging);
+// sp: the pitch of the staged items (every staged item's ldk equals it).
 cudaError_t launch_batch_construct(const ColonyDev *descs, const int4 *items, int num_items,
                                    int *queue_head, int grid, int warps, int max_n, int max_k,
-                                   bool aging, cudaStream_t s);
+                                   size_t region_bytes, int sp, bool aging, cudaStream_t s);
 // Row-owned pheromone pass: optional evaporation, optional ordered deposit
 // of the deposit list, then choice / choice_nn / tau_nn / row means.
 cudaError_t launch_pheromone_rows(const ColonyDev &c, bool evaporate, bool deposit,

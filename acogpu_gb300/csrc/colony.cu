@@ -58,7 +58,8 @@ ColonyDev make_dev(const aco_colony *c) {
   ColonyDev d;
   d.n = c->n; d.m = c->m; d.K = c->K; d.ld = c->ld; d.ldk = c->ldk; d.ldm = c->ldm;
   d.dist = c->dist; d.eta = c->eta; d.tau = c->tau; d.choice = c->choice;
-  d.nn = c->nn; d.eta_nn = c->eta_nn; d.tau_nn = c->tau_nn; d.choice_nn = c->choice_nn;
+  d.nn = c->nn; d.nn16 = c->nn16;
+  d.eta_nn = c->eta_nn; d.tau_nn = c->tau_nn; d.choice_nn = c->choice_nn;
   d.tours = c->tours; d.newlen = c->newlen; d.len = c->len;
   d.succT = c->succT; d.predT = c->predT; d.gbtour = c->gbtour;
   d.age = c->age; d.perf = c->perf; d.valid = c->valid; d.mean = c->mean;
@@ -128,7 +129,7 @@ int allocate(aco_colony *c) {
   if ((s = dalloc(c, &c->valid, m))) return s;
   if ((s = dalloc(c, &c->mean, ld))) return s;
   if (c->K <= 32 && c->n < 32768)
-    if ((s = dalloc(c, &c->nn16, n * 32))) return s;
+    if ((s = dalloc(c, &c->nn16, n * ldk))) return s;
   if ((s = dalloc(c, &c->dep_col, m + 1))) return s;
   if ((s = dalloc(c, &c->dep_delta, m + 1))) return s;
   if ((s = dalloc(c, &c->st, 1))) return s;
@@ -150,7 +151,7 @@ int create_common(const aco_params *params, int32_t n, aco_colony **out, aco_col
   c->m = params->num_ants;
   c->K = (params->cand_k <= 0 || params->cand_k >= n) ? n : params->cand_k;
   c->ld = round_up(n, 32);
-  c->ldk = round_up(c->K, 32);
+  c->ldk = c->K <= 32 ? staged_pitch(c->K) : round_up(c->K, 32);
   c->ldm = round_up(c->m + 1, 32);
   c->apb = params->ants_per_block > 0 ? params->ants_per_block : 4;
   cudaGetDevice(&c->device);
@@ -214,7 +215,7 @@ int plan_construction(aco_colony *c) {
   const int sms = c->num_sms > 0 ? c->num_sms : 1;
   int warps = (c->m + sms - 1) / sms;
   warps = warps < 1 ? 1 : (warps > kStagedMaxWarps ? kStagedMaxWarps : warps);
-  const size_t smem = construct_staged_smem_bytes(c->n, c->ld, c->p.aging != 0, warps);
+  const size_t smem = construct_staged_smem_bytes(c->n, c->ld, c->ldk, c->p.aging != 0, warps);
   if (smem > (size_t)c->max_smem_optin) {
     if (c->p.construct_mode == ACO_CONSTRUCT_STAGED)
       return fail(c, ACO_ERR_UNSUPPORTED, "candidate table does not fit in shared memory");
@@ -757,8 +758,11 @@ struct aco_batch {
   int4 *d_items = nullptr;
   int *d_queue = nullptr;
   int total_rows = 0, num_items = 0;
-  int max_n = 0, max_k = 0, max_ld = 0, num_sms = 1;
+  int max_n = 0, max_k = 0, max_ld = 0, num_sms = 1, max_smem_optin = 0;
+  int sp = 0;  // row pitch of the staged items: the largest among instances with k <= 32
   int apb = 8, row_threads = 256, grid = 0;
+  size_t region_bytes = 0;  // shared region of the construction launch
+  int staged_count = 0;     // instances built from a staged table
   bool initialized = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -796,16 +800,45 @@ cudaError_t upload_sync(aco_batch *b, void *dst, const void *src, size_t bytes) 
   return e == cudaSuccess ? cudaStreamSynchronize(b->stream) : e;
 }
 
-// Work items (instance, first ant, ants, 0), largest instances first.
+// Shared memory of the construction launch with `apb` warps per CTA: the
+// largest staged table that fits next to the per-warp buffers, and which
+// instances are staged.
+size_t batch_plan_region(const aco_batch *b, int apb, std::vector<char> *staged, int *count) {
+  const bool aging = b->p.aging != 0;
+  // static shared memory of the kernel (descriptor, item, flags) plus slack
+  const size_t fixed = sizeof(ColonyDev) + 256;
+  const size_t avail = (size_t)b->max_smem_optin - batch_construct_smem_bytes(0, apb) - fixed;
+  size_t max_table = 0;
+  int cnt = 0;
+  if (staged) staged->assign(b->cols.size(), 0);
+  for (size_t i = 0; i < b->cols.size(); i++) {
+    const aco_colony *c = b->cols[i];
+    if (b->p.construct_mode == ACO_CONSTRUCT_GLOBAL || c->K > 32 || !c->nn16 || c->n > 2048 ||
+        c->ldk != b->sp)
+      continue;
+    const size_t t = batch_staged_table_bytes(c->n, c->ld, b->sp, aging);
+    if (t > avail) continue;
+    max_table = std::max(max_table, t);
+    cnt++;
+    if (staged) (*staged)[i] = 1;
+  }
+  if (count) *count = cnt;
+  return batch_region_bytes(b->max_n, b->max_k, apb, max_table);
+}
+
+// Work items (instance, first ant, ants, staged), largest instances first.
 int batch_build_items(aco_batch *b) {
   std::vector<int> order(b->cols.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int c) { return b->cols[a]->n > b->cols[c]->n; });
+  std::vector<char> staged;
+  b->region_bytes = batch_plan_region(b, b->apb, &staged, &b->staged_count);
   std::vector<int4> items;
   for (int i : order) {
     const int m = b->cols[i]->m;
-    for (int a0 = 0; a0 < m; a0 += b->apb) items.push_back(make_int4(i, a0, std::min(b->apb, m - a0), 0));
+    for (int a0 = 0; a0 < m; a0 += b->apb)
+      items.push_back(make_int4(i, a0, std::min(b->apb, m - a0), staged[i]));
   }
   if (b->d_items) cudaFree(b->d_items);
   b->d_items = nullptr;
@@ -813,9 +846,9 @@ int batch_build_items(aco_batch *b) {
   ACO_BCUDA(b, upload_sync(b, b->d_items, items.data(), items.size() * sizeof(int4)),
             "upload items");
   b->num_items = (int)items.size();
-  const size_t smem = batch_construct_smem_bytes(b->max_n, b->max_k, b->apb);
+  const size_t smem = batch_construct_smem_bytes(b->region_bytes, b->apb);
   ACO_BCUDA(b, configure_batch_construct(smem), "configure batch construct");
-  b->grid = b->num_sms * batch_construct_blocks_per_sm(b->apb, smem, b->max_k > 32,
+  b->grid = b->num_sms * batch_construct_blocks_per_sm(b->apb, smem, b->max_k > 32, b->sp,
                                                        b->p.aging != 0);
   batch_drop_graph(b);
   return ACO_OK;
@@ -825,7 +858,8 @@ int batch_enqueue(aco_batch *b, bool construct, bool epilogue, bool rows, bool u
   if (construct) {
     ACO_BCUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream), "reset queue");
     ACO_BCUDA(b, launch_batch_construct(b->d_descs, b->d_items, b->num_items, b->d_queue, b->grid,
-                                        b->apb, b->max_n, b->max_k, b->p.aging != 0, b->stream),
+                                        b->apb, b->max_n, b->max_k, b->region_bytes, b->sp,
+                                        b->p.aging != 0, b->stream),
               "batch construct");
     b->launches++;
   }
@@ -871,6 +905,7 @@ int aco_batch_create(const aco_params *params, int32_t count, const int32_t *siz
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&b->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   size_t off = 0;
   for (int32_t i = 0; i < count; i++) {
     const int n = sizes[i];
@@ -889,9 +924,11 @@ int aco_batch_create(const aco_params *params, int32_t count, const int32_t *siz
     off += 2 * (size_t)n;
     b->max_n = std::max(b->max_n, c->n);
     b->max_k = std::max(b->max_k, c->K);
+    if (c->K <= 32) b->sp = std::max(b->sp, c->ldk);
     b->max_ld = std::max(b->max_ld, c->ld);
     b->total_rows += n;
   }
+  if (b->sp == 0) b->sp = 32;
   *out = b;
   return ACO_OK;
 }
@@ -963,7 +1000,9 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
   float best_ms = 1e30f;
   int best_apb = b->apb;
   for (int apb : apbs) {
-    if (batch_construct_smem_bytes(b->max_n, b->max_k, apb) > 200 * 1024) continue;
+    if (batch_construct_smem_bytes(batch_plan_region(b, apb, nullptr, nullptr), apb) >
+        (size_t)b->max_smem_optin)
+      continue;
     b->apb = apb;
     if (int s = batch_build_items(b)) return s;
     float ms = 1e30f;
@@ -1019,6 +1058,7 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
     out->row_threads = best_threads;
     out->construct_ms = best_ms;
     out->rows_ms = best_rows;
+    out->staged_instances = b->staged_count;
   }
   return ACO_OK;
 }

@@ -450,20 +450,24 @@ __device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&t
 // uniforms of 32 consecutive steps are computed one per lane and broadcast;
 // the tour positions of the current 32-step block stay in one register per
 // lane and are stored together.
-template <int TW, bool BLEND>
+template <int TW, bool BLEND, int G>
 __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t akey, int start,
                                             uint32_t (&tw)[TW], float *wbuf, const int16_t *sids,
                                             const float *scw, const float *smean, AntCtx a,
                                             int lane, int64_t &fallbacks) {
+  constexpr int SP = 4 * G;  // row pitch of the staged table
   const int n = c.n;
   int32_t *trow = c.tours + (size_t)k * c.ld;
   const float4 *wbuf4 = reinterpret_cast<const float4 *>(wbuf);
-  float incl[32];
+  float incl[SP];
 #pragma unroll
-  for (int e = 0; e < 32; e++) incl[e] = e <= lane ? 1.0f : 0.0f;
+  for (int e = 0; e < SP; e++) incl[e] = e <= lane ? 1.0f : 0.0f;
+  // Lanes past the pitch repeat the last entry: their prefix equals the full
+  // sum, so they are never the first crossing.
+  const int lr = lane < SP ? lane : SP - 1;
   int cur = start;
-  int id = sids[cur * 32 + lane];
-  float wraw = BLEND ? 0.0f : scw[cur * 32 + lane];
+  int id = sids[cur * SP + lr];
+  float wraw = BLEND ? 0.0f : scw[cur * SP + lr];
   bool ok = true;
   for (int xb = 0; xb < n && ok; xb += 32) {
     const float ublk = aco_uniform_key(akey, (uint32_t)(xb + lane));
@@ -490,7 +494,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
       // second fills the first's latency gaps and saves a broadcast).
       float acc = 0.0f, sum = 0.0f;
 #pragma unroll
-      for (int g = 0; g < 8; g++) {
+      for (int g = 0; g < G; g++) {
         const float4 p = wbuf4[g];
         acc = __fmaf_rn(p.x, incl[4 * g + 0], acc);
         sum = __fadd_rn(sum, p.x);
@@ -508,8 +512,8 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
       // stand-in keeps the loads inside the table) and reloaded if the
       // fallback picks the city.
       const int nx = (unsigned)next < (unsigned)n ? next : 0;
-      int id_next = sids[nx * 32 + lane];
-      float w_next = BLEND ? 0.0f : scw[nx * 32 + lane];
+      int id_next = sids[nx * SP + lr];
+      float w_next = BLEND ? 0.0f : scw[nx * SP + lr];
       if (hit == 0u || (unsigned)next >= (unsigned)n) {
         if (hit != 0u) {  // a candidate id outside the instance: recorded, not used
           ok = false;
@@ -525,8 +529,8 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
           if (lane == 0) atomicOr(&c.st->error, kErrCheck);
           break;
         }
-        id_next = sids[next * 32 + lane];
-        w_next = BLEND ? 0.0f : scw[next * 32 + lane];
+        id_next = sids[next * SP + lr];
+        w_next = BLEND ? 0.0f : scw[next * SP + lr];
       }
       reg_mark(tw, next, lane);
       tpos = lane == (x & 31) ? next : tpos;
@@ -539,7 +543,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
   return cur;
 }
 
-template <bool AGING, int TW>
+template <bool AGING, int TW, int G>
 __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
                                      const int16_t *sids, const float *scw, const float *smean,
                                      int lane) {
@@ -578,9 +582,9 @@ __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, f
 
   int64_t fallbacks = 0;
   if (AGING && a.blend)
-    staged_steps<TW, true>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
+    staged_steps<TW, true, G>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
   else
-    staged_steps<TW, false>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
+    staged_steps<TW, false, G>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
   __syncwarp();
   // Tour length (order-free integer sum) and the transposed successor /
   // predecessor of every city for the row-owned deposit, one edge per lane.
@@ -619,24 +623,20 @@ __global__ void __launch_bounds__(512) k_construct(ColonyDev c, int nchunks) {
                                      nullptr, nchunks, lane);
 }
 
-// Shared-memory layout of the staged kernel:
-//   [choice n*32 f32][ids n*32 int16][mean ld f32, aging][per warp: 32 f32][mbarrier]
-__host__ __device__ inline size_t staged_table_bytes(int n, int ld, bool aging) {
-  return (size_t)n * 32 * 4 + (size_t)n * 32 * 2 + (aging ? (size_t)ld * 4 : 0);
-}
-
-template <bool AGING, int TW>
+// Shared-memory layout of the staged kernel: the table of staged_layout,
+// then per warp 32 f32, then the mbarrier.  G = pitch / 4.
+template <bool AGING, int TW, int G>
 __global__ void __launch_bounds__(kStagedMaxWarps * 32)
     k_construct_staged(ColonyDev c, const int16_t *nn16) {
   extern __shared__ __align__(128) unsigned char smem_staged[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
   const int n = c.n;
+  const StagedLayout L = staged_layout(n, c.ld, 4 * G, AGING);
   float *scw = reinterpret_cast<float *>(smem_staged);
-  int16_t *sids = reinterpret_cast<int16_t *>(smem_staged + (size_t)n * 128);
-  float *smean = reinterpret_cast<float *>(smem_staged + (size_t)n * 192);
-  const size_t table = staged_table_bytes(n, c.ld, AGING);  // a multiple of 64 bytes
-  float *wbuf = reinterpret_cast<float *>(smem_staged + table) + (size_t)warp * 32;
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_staged + table + (size_t)warps * 128);
+  int16_t *sids = reinterpret_cast<int16_t *>(smem_staged + L.ids_off);
+  float *smean = reinterpret_cast<float *>(smem_staged + L.mean_off);
+  float *wbuf = reinterpret_cast<float *>(smem_staged + L.table) + (size_t)warp * 32;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_staged + L.table + (size_t)warps * 128);
   __shared__ int flag;
 
   if (threadIdx.x == 0) {
@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const uint32_t cw_bytes = (uint32_t)n * 128u, id_bytes = (uint32_t)n * 64u;
+    const uint32_t cw_bytes = (uint32_t)L.ids_off, id_bytes = (uint32_t)(L.mean_off - L.ids_off);
     const uint32_t mean_bytes = AGING ? (uint32_t)c.ld * 4u : 0u;
     mbar_arrive_expect_tx(bar, cw_bytes + id_bytes + mean_bytes);
     constexpr uint32_t kPiece = 32768;
@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
   if (!flag) return;
   const uint32_t iter = c.st->iteration;
   for (int k = blockIdx.x * warps + warp; k < c.m; k += gridDim.x * warps)
-    construct_ant_staged<AGING, TW>(c, k, iter, wbuf, sids, scw, smean, lane);
+    construct_ant_staged<AGING, TW, G>(c, k, iter, wbuf, sids, scw, smean, lane);
 }
 
 size_t construct_smem_bytes(int n, int K, int ants_per_block) {
@@ -672,8 +672,8 @@ size_t construct_smem_bytes(int n, int K, int ants_per_block) {
   return (size_t)ants_per_block * per_warp * 4;
 }
 
-size_t construct_staged_smem_bytes(int n, int ld, bool aging, int warps) {
-  return staged_table_bytes(n, ld, aging) + (size_t)warps * 128 + 16;
+size_t construct_staged_smem_bytes(int n, int ld, int sp, bool aging, int warps) {
+  return staged_layout(n, ld, sp, aging).table + (size_t)warps * 128 + 16;
 }
 
 cudaError_t configure_construct(size_t smem) {
@@ -689,15 +689,45 @@ cudaError_t configure_construct(size_t smem) {
   return e;
 }
 
+namespace {
+template <bool AGING, int TW, int G>
+cudaError_t staged_attr(int v) {
+  return cudaFuncSetAttribute(k_construct_staged<AGING, TW, G>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+}
+template <int G>
+cudaError_t staged_attr_all(int v) {
+  cudaError_t e = staged_attr<true, 1, G>(v);
+  if (e == cudaSuccess) e = staged_attr<false, 1, G>(v);
+  if (e == cudaSuccess) e = staged_attr<true, 2, G>(v);
+  if (e == cudaSuccess) e = staged_attr<false, 2, G>(v);
+  return e;
+}
+template <int G>
+cudaError_t staged_launch(const ColonyDev &c, const int16_t *nn16, int grid, int warps,
+                          size_t smem, cudaStream_t s) {
+  const bool two = c.n > 1024;
+  if (c.aging) {
+    if (two)
+      k_construct_staged<true, 2, G><<<grid, warps * 32, smem, s>>>(c, nn16);
+    else
+      k_construct_staged<true, 1, G><<<grid, warps * 32, smem, s>>>(c, nn16);
+  } else {
+    if (two)
+      k_construct_staged<false, 2, G><<<grid, warps * 32, smem, s>>>(c, nn16);
+    else
+      k_construct_staged<false, 1, G><<<grid, warps * 32, smem, s>>>(c, nn16);
+  }
+  return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t configure_construct_staged(size_t smem) {
   const int v = (int)smem;
-  cudaError_t e = cudaSuccess;
-  const void *fns[4] = {(const void *)k_construct_staged<true, 1>,
-                        (const void *)k_construct_staged<false, 1>,
-                        (const void *)k_construct_staged<true, 2>,
-                        (const void *)k_construct_staged<false, 2>};
-  for (int i = 0; i < 4 && e == cudaSuccess; i++)
-    e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  cudaError_t e = staged_attr_all<4>(v);
+  if (e == cudaSuccess) e = staged_attr_all<5>(v);
+  if (e == cudaSuccess) e = staged_attr_all<6>(v);
+  if (e == cudaSuccess) e = staged_attr_all<8>(v);
   return e;
 }
 
@@ -720,21 +750,14 @@ cudaError_t launch_construct(const ColonyDev &c, int apb, cudaStream_t s) {
 
 cudaError_t launch_construct_staged(const ColonyDev &c, const int16_t *nn16, int grid, int warps,
                                     cudaStream_t s) {
-  if (c.n > 2048) return cudaErrorInvalidValue;
-  const size_t smem = construct_staged_smem_bytes(c.n, c.ld, c.aging, warps);
-  const bool two = c.n > 1024;
-  if (c.aging) {
-    if (two)
-      k_construct_staged<true, 2><<<grid, warps * 32, smem, s>>>(c, nn16);
-    else
-      k_construct_staged<true, 1><<<grid, warps * 32, smem, s>>>(c, nn16);
-  } else {
-    if (two)
-      k_construct_staged<false, 2><<<grid, warps * 32, smem, s>>>(c, nn16);
-    else
-      k_construct_staged<false, 1><<<grid, warps * 32, smem, s>>>(c, nn16);
+  if (c.n > 2048 || c.K > 32 || c.ldk != staged_pitch(c.K)) return cudaErrorInvalidValue;
+  const size_t smem = construct_staged_smem_bytes(c.n, c.ld, c.ldk, c.aging, warps);
+  switch (c.ldk) {
+    case 16: return staged_launch<4>(c, nn16, grid, warps, smem, s);
+    case 20: return staged_launch<5>(c, nn16, grid, warps, smem, s);
+    case 24: return staged_launch<6>(c, nn16, grid, warps, smem, s);
+    default: return staged_launch<8>(c, nn16, grid, warps, smem, s);
   }
-  return cudaGetLastError();
 }
 
 }  // namespace aco
@@ -743,23 +766,41 @@ namespace aco {
 
 // ---------------------------------------------------------------------------
 // Batches of instances of uneven size in one persistent launch.  Each CTA
-// takes work items -- (instance, first ant, ant count) -- from a global queue
-// with atomicAdd until the queue is empty; no CTA ever waits for another.
-// Items are ordered by decreasing instance size on the host (longest job
-// first), so the tail of the launch is made of small items.  The instance's
-// descriptor is copied into shared memory once per item.
-template <bool MULTI, bool AGING>
+// takes work items -- (instance, first ant, ant count, staged) -- from a
+// global queue with atomicAdd until the queue is empty; no CTA ever waits for
+// another.  Items are ordered by decreasing instance size on the host
+// (longest job first), so the tail of the launch is made of small items.  The
+// instance's descriptor is copied into shared memory once per item.
+//
+// A staged item (k <= 32 and a candidate table that fits the CTA's table
+// region) first copies its instance's table -- FP32 choice values, int16
+// ids, and the aging row means -- into shared memory with TMA bulk copies on
+// one mbarrier, then its warps build tours with the staged step loop of the
+// single-colony kernel.  Other items build tours from L2 rows with the tabu
+// list in the same region.  Shared layout:
+//   [region: table, or per-warp tabu lists][per warp: 32 f32][mbarrier]
+template <bool MULTI, bool AGING, int G>
 __global__ void __launch_bounds__(512) k_batch_construct(const ColonyDev *__restrict__ descs,
                                                          const int4 *__restrict__ items,
                                                          int num_items, int *queue_head,
-                                                         int words, int max_chunks) {
-  extern __shared__ __align__(16) uint32_t smem_bc[];
+                                                         int words, int max_chunks,
+                                                         uint32_t region_bytes) {
+  extern __shared__ __align__(128) unsigned char smem_bc[];
   __shared__ ColonyDev s_desc;
-  __shared__ int s_item;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *tabu = smem_bc + (size_t)warp * (words + 32 + (MULTI ? max_chunks : 0));
+  __shared__ int s_item, s_ok;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+  uint32_t *tabu = reinterpret_cast<uint32_t *>(smem_bc) +
+                   (size_t)warp * (words + 32 + (MULTI ? max_chunks : 0));
   float *wbuf = reinterpret_cast<float *>(tabu + words);
   float *cend = wbuf + 32;
+  float *swbuf = reinterpret_cast<float *>(smem_bc + region_bytes) + (size_t)warp * 32;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_bc + region_bytes + (size_t)warps * 128);
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  uint32_t phase = 0;
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(queue_head, 1);
     __syncthreads();
@@ -769,65 +810,149 @@ __global__ void __launch_bounds__(512) k_batch_construct(const ColonyDev *__rest
     if (threadIdx.x == 0) s_desc = descs[w.x];
     __syncthreads();
     const ColonyDev &c = s_desc;
-    if (warp < w.z)
+    if (!MULTI && w.w) {
+      const int n = c.n;
+      const StagedLayout L = staged_layout(n, c.ld, 4 * G, AGING);
+      float *scw = reinterpret_cast<float *>(smem_bc);
+      int16_t *sids = reinterpret_cast<int16_t *>(smem_bc + L.ids_off);
+      float *smean = reinterpret_cast<float *>(smem_bc + L.mean_off);
+      if (threadIdx.x == 0) {
+        // The previous item's reads of the region (generic proxy) come
+        // before the copies' writes (async proxy).
+        fence_proxy_async();
+        const uint32_t cw_bytes = (uint32_t)L.ids_off;
+        const uint32_t id_bytes = (uint32_t)(L.mean_off - L.ids_off);
+        const uint32_t mean_bytes = AGING ? (uint32_t)c.ld * 4u : 0u;
+        mbar_arrive_expect_tx(bar, cw_bytes + id_bytes + mean_bytes);
+        constexpr uint32_t kPiece = 32768;
+        const char *g = reinterpret_cast<const char *>(c.choice_nn);
+        for (uint32_t o = 0; o < cw_bytes; o += kPiece)
+          tma_load_1d(reinterpret_cast<char *>(scw) + o, g + o, min(kPiece, cw_bytes - o), bar);
+        g = reinterpret_cast<const char *>(c.nn16);
+        for (uint32_t o = 0; o < id_bytes; o += kPiece)
+          tma_load_1d(reinterpret_cast<char *>(sids) + o, g + o, min(kPiece, id_bytes - o), bar);
+        if (AGING) tma_load_1d(smean, c.mean, mean_bytes, bar);
+        bool ok = mbar_wait_bounded(bar, phase, c.st);
+        // After a timeout, wait (bounded again) for the copies still in
+        // flight before the CTA stops taking items.
+        if (!ok) mbar_wait_bounded(bar, phase, c.st);
+        s_ok = ok ? 1 : 0;
+      }
+      phase ^= 1u;
+      __syncthreads();
+      if (!s_ok) break;
+      if (warp < w.z) {
+        if (n <= 1024)
+          construct_ant_staged<AGING, 1, G>(c, w.y + warp, c.st->iteration, swbuf, sids, scw,
+                                            smean, lane);
+        else
+          construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf, sids, scw,
+                                            smean, lane);
+      }
+    } else if (warp < w.z) {
       construct_ant<MULTI, AGING, false>(c, w.y + warp, c.st->iteration, tabu, cend, wbuf,
                                          nullptr, nullptr, nullptr, (c.K + 31) >> 5, lane);
-    __syncthreads();  // s_item and s_desc are rewritten by the next item
+    }
+    __syncthreads();  // s_item, s_desc and the region are rewritten by the next item
   }
 }
 
-size_t batch_construct_smem_bytes(int max_n, int max_k, int warps) {
+// Bytes of the shared region: the largest staged table of the batch, or the
+// per-warp tabu lists of L2-row items, whichever is larger (128-byte
+// multiple).
+size_t batch_region_bytes(int max_n, int max_k, int warps, size_t max_table) {
   const int words = (max_n + 31) / 32;
   const int chunks = (max_k + 31) / 32;
-  return (size_t)warps * (words + 32 + (max_k > 32 ? chunks : 0)) * 4;
+  const size_t tabu = (size_t)warps * (words + 32 + (max_k > 32 ? chunks : 0)) * 4;
+  return ((tabu > max_table ? tabu : max_table) + 127) / 128 * 128;
 }
+
+size_t batch_construct_smem_bytes(size_t region_bytes, int warps) {
+  return region_bytes + (size_t)warps * 128 + 16;
+}
+
+size_t batch_staged_table_bytes(int n, int ld, int sp, bool aging) {
+  return staged_layout(n, ld, sp, aging).table;
+}
+
+namespace {
+template <bool MULTI, bool AGING, int G>
+cudaError_t batch_attr(int v) {
+  return cudaFuncSetAttribute(k_batch_construct<MULTI, AGING, G>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+}
+template <bool MULTI, bool AGING, int G>
+cudaError_t batch_launch(const ColonyDev *descs, const int4 *items, int num_items, int *queue_head,
+                         int grid, int warps, size_t smem, int words, int chunks, uint32_t rb,
+                         cudaStream_t s) {
+  k_batch_construct<MULTI, AGING, G><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
+                                                                   queue_head, words, chunks, rb);
+  return cudaGetLastError();
+}
+template <bool AGING, int G>
+const void *batch_fn(bool multi) {
+  return multi ? (const void *)k_batch_construct<true, AGING, 8>
+               : (const void *)k_batch_construct<false, AGING, G>;
+}
+const void *batch_fn_for(bool multi, int sp, bool aging) {
+  switch (sp) {
+    case 16: return aging ? batch_fn<true, 4>(multi) : batch_fn<false, 4>(multi);
+    case 20: return aging ? batch_fn<true, 5>(multi) : batch_fn<false, 5>(multi);
+    case 24: return aging ? batch_fn<true, 6>(multi) : batch_fn<false, 6>(multi);
+    default: return aging ? batch_fn<true, 8>(multi) : batch_fn<false, 8>(multi);
+  }
+}
+}  // namespace
 
 cudaError_t configure_batch_construct(size_t smem) {
   const int v = (int)smem;
-  const void *fns[4] = {(const void *)k_batch_construct<true, true>,
-                        (const void *)k_batch_construct<true, false>,
-                        (const void *)k_batch_construct<false, true>,
-                        (const void *)k_batch_construct<false, false>};
-  cudaError_t e = cudaSuccess;
-  for (int i = 0; i < 4 && e == cudaSuccess; i++)
-    e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  cudaError_t e = batch_attr<true, true, 8>(v);
+  if (e == cudaSuccess) e = batch_attr<true, false, 8>(v);
+  if (e == cudaSuccess) e = batch_attr<false, true, 4>(v);
+  if (e == cudaSuccess) e = batch_attr<false, false, 4>(v);
+  if (e == cudaSuccess) e = batch_attr<false, true, 5>(v);
+  if (e == cudaSuccess) e = batch_attr<false, false, 5>(v);
+  if (e == cudaSuccess) e = batch_attr<false, true, 6>(v);
+  if (e == cudaSuccess) e = batch_attr<false, false, 6>(v);
+  if (e == cudaSuccess) e = batch_attr<false, true, 8>(v);
+  if (e == cudaSuccess) e = batch_attr<false, false, 8>(v);
   return e;
 }
 
-int batch_construct_blocks_per_sm(int warps, size_t smem, bool multi, bool aging) {
+int batch_construct_blocks_per_sm(int warps, size_t smem, bool multi, int sp, bool aging) {
   int blocks = 0;
-  const void *f = multi ? (aging ? (const void *)k_batch_construct<true, true>
-                                 : (const void *)k_batch_construct<true, false>)
-                        : (aging ? (const void *)k_batch_construct<false, true>
-                                 : (const void *)k_batch_construct<false, false>);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, f, warps * 32, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batch_fn_for(multi, sp, aging),
+                                                    warps * 32, smem) != cudaSuccess)
     return 1;
   return blocks > 0 ? blocks : 1;
 }
 
 cudaError_t launch_batch_construct(const ColonyDev *descs, const int4 *items, int num_items,
                                    int *queue_head, int grid, int warps, int max_n, int max_k,
-                                   bool aging, cudaStream_t s) {
+                                   size_t region_bytes, int sp, bool aging, cudaStream_t s) {
   const int words = (max_n + 31) / 32;
   const int chunks = (max_k + 31) / 32;
-  const size_t smem = batch_construct_smem_bytes(max_n, max_k, warps);
-  const bool multi = max_k > 32;
-  if (multi) {
-    if (aging)
-      k_batch_construct<true, true><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
-                                                                  queue_head, words, chunks);
-    else
-      k_batch_construct<true, false><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
-                                                                   queue_head, words, chunks);
-  } else {
-    if (aging)
-      k_batch_construct<false, true><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
-                                                                   queue_head, words, chunks);
-    else
-      k_batch_construct<false, false><<<grid, warps * 32, smem, s>>>(descs, items, num_items,
-                                                                    queue_head, words, chunks);
+  const size_t smem = batch_construct_smem_bytes(region_bytes, warps);
+  const uint32_t rb = (uint32_t)region_bytes;
+  if (max_k > 32)
+    return aging ? batch_launch<true, true, 8>(descs, items, num_items, queue_head, grid, warps,
+                                               smem, words, chunks, rb, s)
+                 : batch_launch<true, false, 8>(descs, items, num_items, queue_head, grid, warps,
+                                                smem, words, chunks, rb, s);
+#define ACO_BATCH_CASE(PITCH, GG)                                                            \
+  case PITCH:                                                                                \
+    return aging ? batch_launch<false, true, GG>(descs, items, num_items, queue_head, grid,   \
+                                                 warps, smem, words, chunks, rb, s)           \
+                 : batch_launch<false, false, GG>(descs, items, num_items, queue_head, grid,  \
+                                                  warps, smem, words, chunks, rb, s);
+  switch (sp) {
+    ACO_BATCH_CASE(16, 4)
+    ACO_BATCH_CASE(20, 5)
+    ACO_BATCH_CASE(24, 6)
+    default:
+    ACO_BATCH_CASE(32, 8)
   }
-  return cudaGetLastError();
+#undef ACO_BATCH_CASE
 }
 
 }  // namespace aco

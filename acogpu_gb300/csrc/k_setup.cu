@@ -304,15 +304,13 @@ cudaError_t launch_gather_nn_f32(const float *src, int n, int ld, const int32_t 
 
 // int16 copy of a candidate table with 32 entries per row (the staged
 // construction kernel keeps it in shared memory).
+// int16 copy of the candidate rows (same pitch; the -1 padding carries over).
 __global__ void k_nn_to_i16(const int32_t *__restrict__ nn, int n, int ldk,
                             int16_t *__restrict__ nn16) {
-  const int64_t total = (int64_t)n * 32;
+  const int64_t total = (int64_t)n * ldk;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = t >> 5;
-    const int r = (int)(t & 31);
-    nn16[t] = (int16_t)(r < ldk ? nn[j * ldk + r] : -1);
-  }
+       t += (int64_t)gridDim.x * blockDim.x)
+    nn16[t] = (int16_t)nn[t];
 }
 
 cudaError_t launch_nn_to_i16(const int32_t *nn, int n, int ldk, int16_t *nn16, cudaStream_t s) {

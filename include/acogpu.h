@@ -265,7 +265,8 @@ typedef struct aco_tuning {
   int32_t row_threads;    /* threads per CTA of the pheromone row pass */
   float construct_ms;     /* best timed construction launch */
   float rows_ms;          /* best timed row pass */
-  int32_t reserved[4];
+  int32_t staged_instances; /* instances whose candidate table is staged in shared memory */
+  int32_t reserved[3];
 } aco_tuning;
 
 ACO_API int aco_batch_create(const aco_params *params, int32_t count, const int32_t *sizes,
@@ -276,7 +277,10 @@ ACO_API int aco_batch_run(aco_batch *b, int32_t iterations);
 ACO_API int aco_batch_synchronize(aco_batch *b);
 /* Times the construction launch for 1..16 ants per CTA and the row pass for
  * 128..512 threads, keeps the fastest, then returns every instance to its
- * initialised state.  Call after aco_batch_initialize, before running. */
+ * initialised state.  Call after aco_batch_initialize, before running.
+ * Construction: instances with k <= 32 whose candidate table fits in shared
+ * memory (about n <= 1150) are staged there, per work item, unless the batch
+ * parameters ask for ACO_CONSTRUCT_GLOBAL; the others read rows from L2. */
 ACO_API int aco_batch_autotune(aco_batch *b, aco_tuning *out);
 ACO_API int aco_batch_set_tuning(aco_batch *b, int32_t ants_per_block, int32_t row_threads);
 ACO_API int aco_batch_get_size(aco_batch *b, int32_t *count);

@@ -41,10 +41,14 @@ def single(inst, p, i, cap):
 
 @pytest.mark.parametrize("variant,aging", [(_abi.ACO_ANT_SYSTEM, 0), (_abi.ACO_RANK_BASED, 1)])
 @pytest.mark.parametrize("tune", [False, True])
-def test_batch_instances_match_single_colonies(variant, aging, tune):
-    sizes = [57, 120, 333, 64, 210, 95]
+@pytest.mark.parametrize("mode", [_abi.ACO_CONSTRUCT_AUTO, _abi.ACO_CONSTRUCT_GLOBAL],
+                         ids=["staged", "l2rows"])
+def test_batch_instances_match_single_colonies(variant, aging, tune, mode):
+    """Staged items (tables in shared memory) and L2-row items in one launch:
+    the 2000-city table (k = 20: 240 KB) does not fit in shared memory."""
+    sizes = [57, 120, 2000, 333, 64, 1300, 95]
     insts = make_instances(sizes, 300)
-    p = fast_params(variant=variant, rank_w=6, aging=aging)
+    p = fast_params(variant=variant, rank_w=6, aging=aging, construct_mode=mode)
     if aging:
         (p.min_retirement_age, p.max_retirement_age, p.global_performance,
          p.min_population_limit) = (3, 6, 2, 20)
@@ -54,6 +58,7 @@ def test_batch_instances_match_single_colonies(variant, aging, tune):
     if tune:
         t = b.autotune()
         assert t["ants_per_block"] in (1, 2, 4, 8, 16) and t["row_threads"] in (128, 256, 512)
+        assert t["staged_instances"] == (0 if mode == _abi.ACO_CONSTRUCT_GLOBAL else len(sizes) - 1)
     iters = 8
     b.run(iters)
     b.synchronize()
