@@ -203,29 +203,37 @@ int read_state(aco_colony *c, ColonyState *h) {
 cudaError_t launch_construction(aco_colony *c, const ColonyDev &d) {
   if (c->staged)
     return launch_construct_staged(d, c->nn16, c->staged_grid, c->staged_warps, c->stream);
+  if (c->direct) return launch_construct_direct(d, c->staged_grid, c->staged_warps, c->stream);
   return launch_construct(d, c->apb, c->stream);
 }
 
-// Chooses between the staged kernel (whole candidate table in shared
-// memory, one CTA per SM) and the global-memory kernel.
+// Chooses the construction kernel, for k <= 32: the staged kernel (whole
+// candidate table in shared memory, one CTA per SM) when the table fits, else
+// the direct kernel (the same step loop on rows read from L2, n <= 8192);
+// otherwise, and in ACO_CONSTRUCT_GLOBAL mode, the general global-memory
+// kernel.  The first two put one ant per warp, ceil(m / SMs) warps per CTA.
 int plan_construction(aco_colony *c) {
   c->staged = false;
-  if (c->K > 32 || c->n > 2048 || !c->nn16 || c->p.construct_mode == ACO_CONSTRUCT_GLOBAL)
-    return ACO_OK;
+  c->direct = false;
+  if (c->K > 32 || !c->nn16 || c->p.construct_mode == ACO_CONSTRUCT_GLOBAL) return ACO_OK;
   const int sms = c->num_sms > 0 ? c->num_sms : 1;
   int warps = (c->m + sms - 1) / sms;
   warps = warps < 1 ? 1 : (warps > kStagedMaxWarps ? kStagedMaxWarps : warps);
-  const size_t smem = construct_staged_smem_bytes(c->n, c->ld, c->ldk, c->p.aging != 0, warps);
-  if (smem > (size_t)c->max_smem_optin) {
+  int grid = (c->m + warps - 1) / warps;
+  if (grid > sms) grid = sms;
+  c->staged_warps = warps;
+  c->staged_grid = grid;
+  if (c->n <= 2048) {
+    const size_t smem = construct_staged_smem_bytes(c->n, c->ld, c->ldk, c->p.aging != 0, warps);
+    if (smem <= (size_t)c->max_smem_optin) {
+      ACO_CUDA(c, configure_construct_staged(smem), "configure staged construct");
+      c->staged = true;
+      return ACO_OK;
+    }
     if (c->p.construct_mode == ACO_CONSTRUCT_STAGED)
       return fail(c, ACO_ERR_UNSUPPORTED, "candidate table does not fit in shared memory");
-    return ACO_OK;
   }
-  ACO_CUDA(c, configure_construct_staged(smem), "configure staged construct");
-  c->staged = true;
-  c->staged_warps = warps;
-  c->staged_grid = (c->m + warps - 1) / warps;
-  if (c->staged_grid > sms) c->staged_grid = sms;
+  c->direct = c->n <= kDirectMaxCities;
   return ACO_OK;
 }
 

@@ -30,9 +30,10 @@ struct aco_colony {
   int32_t *dep_col = nullptr;
   float *dep_delta = nullptr;
   aco::ColonyState *st = nullptr;
-  int16_t *nn16 = nullptr;  // candidate ids as int16, 32 per row (staged kernel)
+  int16_t *nn16 = nullptr;  // candidate ids as int16, pitch ldk (k <= 32 kernels)
   float *xy = nullptr;      // coordinates (x then y) when created from coordinates
-  bool staged = false;
+  bool staged = false;      // construction by the staged kernel
+  bool direct = false;      // construction by the direct (L2-row) kernel
   int staged_grid = 0, staged_warps = 0;
   int num_sms = 0, max_smem_optin = 0;
   std::vector<void *> allocations;

@@ -327,34 +327,55 @@ __device__ void construct_ant(const ColonyDev &c, int k, uint32_t iter, uint32_t
 // owner lane sets the bit), the non-zero weights compacted into a
 // zero-padded 32-float buffer and folded in lane order from broadcast
 // 16-byte reads.
+// TW words per lane cover 1024*TW cities: word w of the tabu list is held
+// by lane w % 32 as its register w / 32.  A city past the list (a padding id)
+// reads as unvisited.
 template <int TW>
 __device__ __forceinline__ bool reg_visited(const uint32_t (&tw)[TW], int city) {
   const int word = city >> 5;
   uint32_t v = __shfl_sync(kFull, tw[0], word & 31);
-  if (TW > 1) {
-    const uint32_t v1 = __shfl_sync(kFull, tw[TW > 1 ? 1 : 0], word & 31);
-    v = (word >> 5) ? v1 : v;
+#pragma unroll
+  for (int t = 1; t < TW; t++) {
+    const uint32_t x = __shfl_sync(kFull, tw[t], word & 31);
+    v = (word >> 5) == t ? x : v;
   }
+  if (TW > 1 && (word >> 5) >= TW) v = 0u;
   return (v >> (city & 31)) & 1u;
 }
 
+// Every register is updated (with the bit or with 0), so the compiler never
+// turns the update into a store at a computed index.
 template <int TW>
 __device__ __forceinline__ void reg_mark(uint32_t (&tw)[TW], int city, int lane) {
   const int word = city >> 5;
-  if (lane == (word & 31)) {
-    if (TW == 1 || (word >> 5) == 0)
-      tw[0] |= 1u << (city & 31);
-    else
-      tw[TW > 1 ? 1 : 0] |= 1u << (city & 31);
+  const uint32_t bit = lane == (word & 31) ? 1u << (city & 31) : 0u;
+  if (TW == 1) {  // every city is below 1024
+    tw[0] |= bit;
+    return;
   }
+#pragma unroll
+  for (int t = 0; t < TW; t++) tw[t] |= (word >> 5) == t ? bit : 0u;
+}
+
+// Register t of the tabu words, t uniform across the warp (a select chain,
+// so the array never needs a dynamic index).
+template <int TW>
+__device__ __forceinline__ uint32_t tw_pick(const uint32_t (&tw)[TW], int t) {
+  uint32_t v = tw[0];
+#pragma unroll
+  for (int i = 1; i < TW; i++) v = t == i ? tw[i] : v;
+  return v;
 }
 
 // Largest choice value among unvisited cities (register tabu version).  The
 // plain rule issues the row loads four 128-city chunks at a time, so a scan
 // of n cities waits for ceil(n / 512) L2 round trips, not one per chunk.
+// Inlined: the tabu words must stay in registers (a call would take the
+// array's address and move it to local memory).
 template <int TW>
-__device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&tw)[TW],
-                                 const AntCtx &a, int lane) {
+__device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
+                                                 const uint32_t (&tw)[TW], const AntCtx &a,
+                                                 int lane) {
   float bw = -1.0f;
   int bj = -1;
   const float *crow = c.choice + (size_t)cur * c.ld;
@@ -363,7 +384,7 @@ __device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&t
   if (!a.blend) {
 #pragma unroll
     for (int t0 = 0; t0 < 8 * TW; t0 += 4) {  // n <= 1024 * TW
-      if (t0 * 128 >= c.n) break;
+      if (t0 * 128 >= c.n) continue;  // (not break: the loop stays fully unrolled)
       float4 q[4];
 #pragma unroll
       for (int t = 0; t < 4; t++) {
@@ -375,7 +396,7 @@ __device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&t
       for (int t = 0; t < 4; t++) {
         const int j4 = (t0 + t) * 128 + lane * 4;
         const uint32_t v =
-            __shfl_sync(kFull, tw[(t0 + t) >> 3], ((t0 + t) * 4 + (lane >> 3)) & 31);
+            __shfl_sync(kFull, tw_pick(tw, (t0 + t) >> 3), ((t0 + t) * 4 + (lane >> 3)) & 31);
         const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
         const float qq[4] = {q[t].x, q[t].y, q[t].z, q[t].w};
 #pragma unroll
@@ -390,12 +411,8 @@ __device__ int fallback_best_reg(const ColonyDev &c, int cur, const uint32_t (&t
   } else {  // aging blend (young ants after convergence): tau and eta rows
     for (int base = 0; base < c.n; base += 128) {
       const int j4 = base + lane * 4;
-      const int word = j4 >> 5;  // warp-uniform source per lane group
-      uint32_t v = __shfl_sync(kFull, tw[0], word & 31);
-      if (TW > 1) {
-        const uint32_t v1 = __shfl_sync(kFull, tw[TW > 1 ? 1 : 0], word & 31);
-        v = (word >> 5) ? v1 : v;
-      }
+      const int word = j4 >> 5;  // register word >> 5 (uniform), lane word & 31
+      const uint32_t v = __shfl_sync(kFull, tw_pick(tw, word >> 5), word & 31);
       if (j4 >= c.n) continue;
       const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
       if (bits == 0xfu) continue;
@@ -665,6 +682,50 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
     construct_ant_staged<AGING, TW, G>(c, k, iter, wbuf, sids, scw, smean, lane);
 }
 
+// k <= 32 with a candidate table too large for shared memory (e.g. n = 4096,
+// k = 32: 768 KB): the staged step loop reading its rows straight from L2
+// (the same pitch-`4G` choice values and int16 ids), the tabu list in
+// registers (TW words per lane, n <= 1024 * TW).
+template <bool AGING, int TW, int G>
+__global__ void __launch_bounds__(kStagedMaxWarps * 32) k_construct_direct(ColonyDev c) {
+  __shared__ __align__(16) float wb[kStagedMaxWarps * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+  const uint32_t iter = c.st->iteration;
+  for (int k = blockIdx.x * warps + warp; k < c.m; k += gridDim.x * warps)
+    construct_ant_staged<AGING, TW, G>(c, k, iter, wb + warp * 32, c.nn16, c.choice_nn, c.mean,
+                                       lane);
+}
+
+namespace {
+template <bool AGING, int G>
+cudaError_t direct_launch_tw(const ColonyDev &c, int grid, int warps, cudaStream_t s) {
+  if (c.n <= 2048)
+    k_construct_direct<AGING, 2, G><<<grid, warps * 32, 0, s>>>(c);
+  else if (c.n <= 4096)
+    k_construct_direct<AGING, 4, G><<<grid, warps * 32, 0, s>>>(c);
+  else
+    k_construct_direct<AGING, 8, G><<<grid, warps * 32, 0, s>>>(c);
+  return cudaGetLastError();
+}
+template <int G>
+cudaError_t direct_launch(const ColonyDev &c, int grid, int warps, cudaStream_t s) {
+  return c.aging ? direct_launch_tw<true, G>(c, grid, warps, s)
+                 : direct_launch_tw<false, G>(c, grid, warps, s);
+}
+}  // namespace
+
+cudaError_t launch_construct_direct(const ColonyDev &c, int grid, int warps, cudaStream_t s) {
+  if (c.n > kDirectMaxCities || c.K > 32 || c.ldk != staged_pitch(c.K) || !c.nn16 ||
+      warps < 1 || warps > kStagedMaxWarps)
+    return cudaErrorInvalidValue;
+  switch (c.ldk) {
+    case 16: return direct_launch<4>(c, grid, warps, s);
+    case 20: return direct_launch<5>(c, grid, warps, s);
+    case 24: return direct_launch<6>(c, grid, warps, s);
+    default: return direct_launch<8>(c, grid, warps, s);
+  }
+}
+
 size_t construct_smem_bytes(int n, int K, int ants_per_block) {
   const int words = (n + 31) / 32;
   const int nchunks = (K + 31) / 32;
@@ -776,8 +837,9 @@ namespace aco {
 // region) first copies its instance's table -- FP32 choice values, int16
 // ids, and the aging row means -- into shared memory with TMA bulk copies on
 // one mbarrier, then its warps build tours with the staged step loop of the
-// single-colony kernel.  Other items build tours from L2 rows with the tabu
-// list in the same region.  Shared layout:
+// single-colony kernel.  Other items with the same pitch (n <= 2048) run that
+// step loop on rows read from L2; the rest use the general kernel with the
+// tabu list in the region.  Shared layout:
 //   [region: table, or per-warp tabu lists][per warp: 32 f32][mbarrier]
 template <bool MULTI, bool AGING, int G>
 __global__ void __launch_bounds__(512) k_batch_construct(const ColonyDev *__restrict__ descs,
@@ -849,6 +911,11 @@ __global__ void __launch_bounds__(512) k_batch_construct(const ColonyDev *__rest
           construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf, sids, scw,
                                             smean, lane);
       }
+    } else if (!MULTI && c.nn16 && c.ldk == 4 * G && c.n <= 2048) {
+      // Too large to stage: the same step loop on rows read from L2.
+      if (warp < w.z)
+        construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf, c.nn16,
+                                          c.choice_nn, c.mean, lane);
     } else if (warp < w.z) {
       construct_ant<MULTI, AGING, false>(c, w.y + warp, c.st->iteration, tabu, cend, wbuf,
                                          nullptr, nullptr, nullptr, (c.K + 31) >> 5, lane);

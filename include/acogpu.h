@@ -99,8 +99,10 @@ enum aco_tau0_mode {
 };
 
 enum aco_construct_mode {
-  ACO_CONSTRUCT_AUTO = 0,   /* staged when the candidate table fits in shared memory */
-  ACO_CONSTRUCT_GLOBAL = 1, /* candidate rows read from global memory (L2) */
+  ACO_CONSTRUCT_AUTO = 0,   /* k <= 32: staged when the candidate table fits in shared
+                               memory, else the same step loop on rows read from L2
+                               (n <= 8192); otherwise the general kernel */
+  ACO_CONSTRUCT_GLOBAL = 1, /* the general kernel: candidate rows read from global memory */
   ACO_CONSTRUCT_STAGED = 2  /* whole candidate table in shared memory; k <= 32 */
 };
 

@@ -140,6 +140,19 @@ def test_construct_kernels_match_oracle(mode, aging):
     run_pair(p, d, 12 if aging else 5, ctx=f"mode{mode}")
 
 
+@pytest.mark.parametrize("n,k,aging", [(1500, 32, 0), (3000, 20, 1), (5000, 32, 0)])
+def test_direct_kernel_matches_oracle(n, k, aging):
+    """k <= 32 with a candidate table too large for shared memory: the step
+    loop on rows read from L2, with the tabu list in 2, 4 and 8 registers per
+    lane, reproduces the oracle (aging: through the blend and its fallback)."""
+    _, _, d = instance(n, 50 + n, kind="clustered")
+    p = params(num_ants=24, beta=2.0, rho=0.2, cand_k=k, seed=n, aging=aging, **FAST_MODE)
+    if aging:
+        (p.min_retirement_age, p.max_retirement_age, p.global_performance,
+         p.min_population_limit) = (3, 6, 2, 20)
+    run_pair(p, d, 10 if aging else 3, ctx=f"direct n{n}")
+
+
 @pytest.mark.parametrize("apb", [1, 2, 8, 16])
 def test_ants_per_block_does_not_change_results(apb):
     _, _, d = instance(66, 4)
