@@ -319,53 +319,71 @@ cudaError_t launch_nn_to_i16(const int32_t *nn, int n, int ldk, int16_t *nn16, c
 }
 
 // ---------------------------------------------------------------- tau0
-// Greedy nearest-neighbour tour from city 0 (lowest index on ties), one
-// warp; then tau0 by the requested rule.  The reference's greedyDistance is a
-// stub returning 0 (src/Colony.cu:1053-1055) and its tau0 is the constant
-// 1e-6 (src/AntSystem.cu:200-203).
-__global__ void k_greedy_tau0(ColonyDev c, int tau0_mode, float tau0_value) {
+// Greedy nearest-neighbour tour from city 0 (lowest index on ties); then tau0
+// by the requested rule.  The reference's greedyDistance is a stub returning
+// 0 (src/Colony.cu:1053-1055) and its tau0 is the constant 1e-6
+// (src/AntSystem.cu:200-203).  One CTA of kGreedyThreads: each step reads the
+// current row once (coalesced, n / kGreedyThreads cities per thread) and takes
+// the block-wide minimum of (distance << 32 | city) over unvisited cities, so
+// a step costs one L2 round trip and two barriers.
+constexpr int kGreedyThreads = 1024;
+
+__global__ void __launch_bounds__(kGreedyThreads)
+    k_greedy_tau0(ColonyDev c, int tau0_mode, float tau0_value) {
   extern __shared__ uint32_t tabu[];
-  const int lane = threadIdx.x;
+  __shared__ unsigned long long red[kGreedyThreads / 32];
+  __shared__ int s_next;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int words = (c.n + 31) >> 5;
   if (tau0_mode != ACO_TAU0_DORIGO) {
-    if (lane == 0) {
+    if (tid == 0) {
       c.st->tau0 = tau0_mode == ACO_TAU0_REFERENCE ? (float)0.000001 : tau0_value;
       c.st->greedy_length = 0;
     }
     return;
   }
-  for (int w = lane; w < words; w += 32) tabu[w] = 0;
-  __syncwarp();
-  if (lane == 0) tabu[0] |= 1u;
-  __syncwarp();
+  for (int w = tid; w < words; w += kGreedyThreads) tabu[w] = w == 0 ? 1u : 0u;
+  __syncthreads();
   int cur = 0;
-  int64_t len = 0;
+  int64_t len = 0;  // kept by thread 0
   for (int s = 1; s < c.n; s++) {
-    int32_t bd = 0x7fffffff;
-    int bj = -1;
-    for (int j = lane; j < c.n; j += 32) {
+    const int32_t *row = c.dist + (size_t)cur * c.ld;
+    unsigned long long best = ~0ull;
+    for (int j = tid; j < c.n; j += kGreedyThreads) {
       if ((tabu[j >> 5] >> (j & 31)) & 1u) continue;
-      const int32_t d = c.dist[(size_t)cur * c.ld + j];
-      if (bj < 0 || d < bd) {
-        bd = d;
-        bj = j;
-      }
+      const unsigned long long key =
+          ((unsigned long long)(uint32_t)__ldcg(row + j) << 32) | (uint32_t)j;
+      best = key < best ? key : best;
     }
     for (int o = 16; o; o >>= 1) {
-      const int32_t od = __shfl_xor_sync(kFull, bd, o);
-      const int oj = __shfl_xor_sync(kFull, bj, o);
-      if (oj >= 0 && (bj < 0 || od < bd || (od == bd && oj < bj))) {
-        bd = od;
-        bj = oj;
+      const unsigned long long other = __shfl_xor_sync(kFull, best, o);
+      best = other < best ? other : best;
+    }
+    if (lane == 0) red[warp] = best;
+    __syncthreads();
+    if (warp == 0) {
+      best = red[lane];
+      for (int o = 16; o; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(kFull, best, o);
+        best = other < best ? other : best;
+      }
+      if (lane == 0) {
+        const int bj = (int)(uint32_t)best;
+        if (best == ~0ull || bj >= c.n) {  // cannot happen with n >= 2; recorded
+          atomicOr(&c.st->error, kErrCheck);
+          s_next = 0;
+        } else {
+          tabu[bj >> 5] |= 1u << (bj & 31);
+          len += (int64_t)(best >> 32);
+          s_next = bj;
+        }
       }
     }
-    len += bd;
-    if (lane == 0) tabu[bj >> 5] |= 1u << (bj & 31);
-    __syncwarp();
-    cur = bj;
+    __syncthreads();
+    cur = s_next;
   }
-  len += c.dist[(size_t)cur * c.ld + 0];
-  if (lane == 0) {
+  if (tid == 0) {
+    len += c.dist[(size_t)cur * c.ld + 0];
     const float cnn = __ll2float_rn(len);
     float t0;
     if (c.variant == ACO_RANK_BASED) {
@@ -382,7 +400,7 @@ __global__ void k_greedy_tau0(ColonyDev c, int tau0_mode, float tau0_value) {
 cudaError_t launch_greedy_tau0(const ColonyDev &c, int tau0_mode, float tau0_value,
                                cudaStream_t s) {
   const size_t smem = (size_t)((c.n + 31) / 32) * 4;
-  k_greedy_tau0<<<1, 32, smem, s>>>(c, tau0_mode, tau0_value);
+  k_greedy_tau0<<<1, kGreedyThreads, smem, s>>>(c, tau0_mode, tau0_value);
   return cudaGetLastError();
 }
 
