@@ -16,6 +16,8 @@ ACO_ERR_NOT_INITIALIZED = 4
 ACO_ERR_UNSUPPORTED = 5
 ACO_ERR_DEVICE_TIMEOUT = 6
 ACO_ERR_DEVICE_CHECK = 7
+ACO_ERR_IO = 8
+ACO_ERR_FORMAT = 9
 
 ACO_ANT_SYSTEM, ACO_RANK_BASED = 0, 1
 ACO_NN_STABLE, ACO_NN_REFERENCE_QSORT = 0, 1
@@ -118,3 +120,22 @@ def default_params(**overrides):
 def aging_six(p):
     return (p.min_retirement_age, p.max_retirement_age, p.local_performance,
             p.global_performance, p.min_population_limit, p.max_population_limit)
+
+
+class IterationStats(ctypes.Structure):
+    """aco_iteration_stats: the reference's Statistics (inc/Statistics.h)."""
+    _fields_ = [("ants", ctypes.c_int32), ("iter", ctypes.c_int32),
+                ("iterbest", ctypes.c_int64), ("globalbest", ctypes.c_int64)] + [
+        (name, ctypes.c_float) for name in (
+            "t_inittour", "t_computeprob", "t_tour", "t_antdist", "t_evapphoremone",
+            "t_updatephoremone", "t_itertime", "t_globaltime")]
+
+
+class RunSummary(ctypes.Structure):
+    """aco_run_summary: the reference's SummaryStatistics without its strings."""
+    _fields_ = [("numcities", ctypes.c_int32), ("numants", ctypes.c_int32),
+                ("numiter", ctypes.c_int32)] + [
+        (name, ctypes.c_float) for name in (
+            "t_inittime", "t_inittour", "t_computeprob", "t_tour", "t_antdist", "t_distcalc",
+            "t_updatephoremone", "t_evappheromnes", "t_totaltime", "d_optimal", "d_calulated",
+            "d_error", "p_alpha", "p_beta", "p_rho")]

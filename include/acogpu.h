@@ -51,7 +51,9 @@ enum aco_status {
   ACO_ERR_NOT_INITIALIZED = 4,
   ACO_ERR_UNSUPPORTED = 5,
   ACO_ERR_DEVICE_TIMEOUT = 6, /* a bounded device-side wait gave up */
-  ACO_ERR_DEVICE_CHECK = 7    /* a device-side consistency check failed */
+  ACO_ERR_DEVICE_CHECK = 7,   /* a device-side consistency check failed */
+  ACO_ERR_IO = 8,             /* a file could not be opened or read */
+  ACO_ERR_FORMAT = 9          /* a file is not in a supported format */
 };
 
 /* ---- parameter enums ----------------------------------------------------- */
@@ -376,6 +378,78 @@ ACO_API int aco_nn_list_reference_order_noalloc(const int32_t *dist_dev, int32_t
 ACO_API const char *aco_colony_last_error(const aco_colony *c);
 ACO_API const char *aco_status_string(int status);
 ACO_API void aco_colony_destroy(aco_colony *c);
+
+/* ---- run loop ------------------------------------------------------------
+ * aco_execute replaces TSP::execute (src/TSP.cpp:23-79), without its file
+ * output: setOptimum, initialize (timed on the host: t_inittime, ms), then
+ * aco_colony_construct_solution with the stage timers while not
+ *   t_totaltime >= max_time || iter >= max_iter || reps >= max_reps ||
+ *   (float)iteration best <= (float)optimum
+ * (TSP::terminationCondition, src/TSP.cpp:166-170; t_totaltime is the sum of
+ * the stage timers in ms; reps is always 0, as in the reference).  stats, if
+ * not null, receives the Statistics of the first stats_cap iterations
+ * (TSP::computeStatistics, src/TSP.cpp:124-149); summary the
+ * SummaryStatistics (src/TSP.cpp:81-122), with d_error =
+ * (d_calulated - d_optimal) / d_optimal * 100 in float (inc/def.h:76). */
+typedef struct aco_iteration_stats { /* Statistics, inc/Statistics.h:17-30 */
+  int32_t ants;
+  int32_t iter;
+  int64_t iterbest;
+  int64_t globalbest;
+  float t_inittour;
+  float t_computeprob;
+  float t_tour;
+  float t_antdist;
+  float t_evapphoremone;
+  float t_updatephoremone;
+  float t_itertime;
+  float t_globaltime;
+} aco_iteration_stats;
+
+typedef struct aco_run_summary { /* SummaryStatistics, inc/Statistics.h:32-53,
+                                    without the platform and file-name strings */
+  int32_t numcities;
+  int32_t numants;
+  int32_t numiter;
+  float t_inittime;
+  float t_inittour;
+  float t_computeprob;
+  float t_tour;
+  float t_antdist;
+  float t_distcalc;
+  float t_updatephoremone;
+  float t_evappheromnes;
+  float t_totaltime;
+  float d_optimal;
+  float d_calulated;
+  float d_error;
+  float p_alpha;
+  float p_beta;
+  float p_rho;
+} aco_run_summary;
+
+ACO_API int aco_execute(aco_colony *c, int32_t max_time, int32_t max_iter, int32_t max_reps,
+                        int32_t optimum, float calcdisttime, aco_iteration_stats *stats,
+                        int32_t stats_cap, aco_run_summary *summary);
+
+/* ---- TSPLIB instances --------------------------------------------------------
+ * aco_tsplib_read replaces TSPReader::read (src/TSPReader.cu:25-95): TYPE TSP
+ * or STSP, EDGE_WEIGHT_TYPE EUC_2D, DIMENSION, then NODE_COORD_SECTION lines
+ * "id x y" read as "%ld %f %f" (float coordinates).  Files the reference would
+ * read past (no DIMENSION before the coordinates, a short or unreadable
+ * coordinate section) give ACO_ERR_FORMAT; an unopenable file ACO_ERR_IO.  The
+ * getters replace TSPReader::getNumNodes / getName / getXcoords / getYcoords
+ * (src/TSPReader.cu:97-118); the arrays live until aco_tsplib_destroy.  Feed
+ * them to aco_colony_create_coords (the distances of src/Setup.cpp:54-70). */
+typedef struct aco_tsplib aco_tsplib;
+ACO_API int aco_tsplib_read(const char *path, aco_tsplib **out);
+ACO_API int32_t aco_tsplib_num_nodes(const aco_tsplib *t);
+ACO_API const char *aco_tsplib_name(const aco_tsplib *t);
+ACO_API const float *aco_tsplib_xcoords(const aco_tsplib *t);
+ACO_API const float *aco_tsplib_ycoords(const aco_tsplib *t);
+/* Message of the calling thread's last failed aco_tsplib_read. */
+ACO_API const char *aco_tsplib_last_error(void);
+ACO_API void aco_tsplib_destroy(aco_tsplib *t);
 
 #ifdef __cplusplus
 }
