@@ -259,6 +259,18 @@ class Colony:
         each city (src/Colony.cu:1173-1180)."""
         return "".join(f"{c + 1}," for c in self.best_tour())
 
+    # -- checkpoint / resume
+    def save(self, path):
+        """Writes the state the next iterations depend on (aco_colony_save)."""
+        self._L.aco_colony_save.argtypes = [_vp, ctypes.c_char_p]
+        self._check(self._L.aco_colony_save(self._h, str(path).encode()), "save")
+
+    def load(self, path):
+        """Restores a checkpoint of the same instance and parameters into this
+        initialized colony; it then continues bit for bit (aco_colony_load)."""
+        self._L.aco_colony_load.argtypes = [_vp, ctypes.c_char_p]
+        self._check(self._L.aco_colony_load(self._h, str(path).encode()), "load")
+
     # -- aging surface (inc/Colony.h:128-139)
     def set_aging_params(self, six):
         a = np.ascontiguousarray(six, dtype=np.int32)

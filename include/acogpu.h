@@ -217,6 +217,19 @@ ACO_API int aco_colony_set_aging_params(aco_colony *c, const int32_t six[6]);
 /* antSystemName(): "Ant System" or "Rank-based Ant System". */
 ACO_API const char *aco_colony_name(const aco_colony *c);
 
+/* Checkpoint / resume (the reference has none).  aco_colony_save writes the
+ * state a colony's next iterations depend on -- pheromone, the device state
+ * block (bests, iteration counter of the random stream, aging flags), the
+ * best-so-far tour and its successor/predecessor lists, the aging arrays,
+ * the last tours and lengths and the candidate heuristic -- with the
+ * parameters and a hash of the distances.  aco_colony_load restores it into
+ * an initialized colony of the same instance and parameters (otherwise
+ * ACO_ERR_INVALID_ARGUMENT; a damaged file ACO_ERR_FORMAT; file errors
+ * ACO_ERR_IO); the loaded colony then continues bit for bit as the saved one
+ * would have. */
+ACO_API int aco_colony_save(aco_colony *c, const char *path);
+ACO_API int aco_colony_load(aco_colony *c, const char *path);
+
 /* State export/import (host buffers), for checking and checkpointing. */
 ACO_API int aco_colony_read_pheromone(aco_colony *c, float *out_nn);      /* n*n */
 ACO_API int aco_colony_write_pheromone(aco_colony *c, const float *in_nn);
