@@ -61,6 +61,9 @@ size_t construct_staged_smem_bytes(int n, int ld, int sp, bool aging, int warps)
 cudaError_t configure_construct_staged(size_t smem);
 cudaError_t launch_construct_staged(const ColonyDev &c, const int16_t *nn16, int grid, int warps,
                                     cudaStream_t s);
+// Aging colonies: the age update and the ants' roles that the staged kernel
+// reads (launched right before it).
+cudaError_t launch_aging_plan(const ColonyDev &c, cudaStream_t s);
 // k <= 32, rows read from L2 by the staged step loop (n <= kDirectMaxCities).
 constexpr int kDirectMaxCities = 8192;
 cudaError_t launch_construct_direct(const ColonyDev &c, int grid, int warps, cudaStream_t s);

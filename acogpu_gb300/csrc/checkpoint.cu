@@ -149,6 +149,7 @@ int aco_colony_save(aco_colony *c, const char *path) {
 
 int aco_colony_load(aco_colony *c, const char *path) {
   if (!c || !path) return ACO_ERR_INVALID_ARGUMENT;
+  state_changed(c);
   if (!c->initialized) return colony_fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
   File f;
   f.f = fopen(path, "rb");

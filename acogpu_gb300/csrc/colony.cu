@@ -63,7 +63,7 @@ ColonyDev make_dev(const aco_colony *c) {
   d.tours = c->tours; d.newlen = c->newlen; d.len = c->len;
   d.succT = c->succT; d.predT = c->predT; d.gbtour = c->gbtour;
   d.age = c->age; d.perf = c->perf; d.valid = c->valid; d.mean = c->mean;
-  d.dep_col = c->dep_col; d.dep_delta = c->dep_delta; d.st = c->st;
+  d.dep_col = c->dep_col; d.dep_delta = c->dep_delta; d.plan = c->plan; d.st = c->st;
   d.rho = c->p.rho; d.alpha = c->p.alpha; d.use_alpha = c->p.use_alpha;
   d.aging = c->p.aging; d.min_ret = c->p.min_retirement_age;
   d.max_ret = c->p.max_retirement_age; d.global_perf = c->p.global_performance;
@@ -130,6 +130,7 @@ int allocate(aco_colony *c) {
   if ((s = dalloc(c, &c->mean, ld))) return s;
   if (c->K <= 32 && c->n < 32768)
     if ((s = dalloc(c, &c->nn16, n * ldk))) return s;
+  if ((s = dalloc(c, &c->plan, m + 1))) return s;
   if ((s = dalloc(c, &c->dep_col, m + 1))) return s;
   if ((s = dalloc(c, &c->dep_delta, m + 1))) return s;
   if ((s = dalloc(c, &c->st, 1))) return s;
@@ -164,6 +165,11 @@ int create_common(const aco_params *params, int32_t n, aco_colony **out, aco_col
   }
   c->own_stream = true;
   for (int i = 0; i < 4; i++) cudaEventCreate(&c->ev[i]);
+  if (cudaMallocHost(&c->h_state, sizeof(ColonyState)) != cudaSuccess) {
+    c->h_state = nullptr;
+    aco_colony_destroy(c);
+    return ACO_ERR_OUT_OF_MEMORY;
+  }
   *cp = c;
   if ((s = allocate(c))) {
     aco_colony_destroy(c);
@@ -194,15 +200,28 @@ int device_error(aco_colony *c) {
 
 int read_state(aco_colony *c, ColonyState *h) {
   if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
-  ACO_CUDA(c, cudaMemcpyAsync(h, c->st, sizeof(*h), cudaMemcpyDeviceToHost, c->stream),
-           "read state");
-  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  if (!c->state_fresh) {
+    ACO_CUDA(c, cudaMemcpyAsync(c->h_state, c->st, sizeof(*h), cudaMemcpyDeviceToHost, c->stream),
+             "read state");
+    ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+    c->state_fresh = true;
+  }
+  *h = *c->h_state;
   return ACO_OK;
 }
 
+// Launches of one construction: the staged kernel of an aging colony is
+// preceded by the plan of the ants' roles.
+int construction_launches(const aco_colony *c) { return c->staged && c->p.aging ? 2 : 1; }
+
 cudaError_t launch_construction(aco_colony *c, const ColonyDev &d) {
-  if (c->staged)
+  if (c->staged) {
+    if (c->p.aging) {
+      cudaError_t e = launch_aging_plan(d, c->stream);
+      if (e != cudaSuccess) return e;
+    }
     return launch_construct_staged(d, c->nn16, c->staged_grid, c->staged_warps, c->stream);
+  }
   if (c->direct) return launch_construct_direct(d, c->staged_grid, c->staged_warps, c->stream);
   return launch_construct(d, c->apb, c->stream);
 }
@@ -223,8 +242,19 @@ int plan_construction(aco_colony *c) {
   if (grid > sms) grid = sms;
   c->staged_warps = warps;
   c->staged_grid = grid;
+  if (c->p.aging && c->n <= 2048) {
+    // All SMs; up to min(m, min_ret) of them may run blend ants (one ant
+    // recruited per iteration blends for min_ret iterations), and the
+    // others' ants must fit in the remaining CTAs' warps.
+    const int young = std::min(c->m, std::max(0, c->p.min_retirement_age));
+    const int rest = std::max(1, sms - young);
+    warps = (c->m + rest - 1) / rest;
+    c->staged_warps = warps < 1 ? 1 : (warps > kStagedMaxWarps ? kStagedMaxWarps : warps);
+    c->staged_grid = sms;
+  }
   if (c->n <= 2048) {
-    const size_t smem = construct_staged_smem_bytes(c->n, c->ld, c->ldk, c->p.aging != 0, warps);
+    const size_t smem =
+        construct_staged_smem_bytes(c->n, c->ld, c->ldk, c->p.aging != 0, c->staged_warps);
     if (smem <= (size_t)c->max_smem_optin) {
       ACO_CUDA(c, configure_construct_staged(smem), "configure staged construct");
       c->staged = true;
@@ -245,10 +275,10 @@ int enqueue_iteration(aco_colony *c) {
     ACO_CUDA(c, launch_evaporate(d, c->stream), "evaporate");
     ACO_CUDA(c, launch_deposit_atomic(d, c->stream), "deposit");
     ACO_CUDA(c, launch_pheromone_rows(d, false, false, false, c->stream), "choice rows");
-    c->launches += 5;
+    c->launches += 4 + construction_launches(c);
   } else {
     ACO_CUDA(c, launch_pheromone_rows(d, true, true, true, c->stream), "pheromone rows");
-    c->launches += 3;
+    c->launches += 2 + construction_launches(c);
   }
   return ACO_OK;
 }
@@ -351,6 +381,7 @@ int aco_colony_create_coords(const aco_params *params, const float *x, const flo
 }
 
 int aco_colony_initialize(aco_colony *c) {
+  if (c) state_changed(c);
   if (!c) return ACO_ERR_INVALID_ARGUMENT;
   drop_graph(c);
   c->initialized = false;
@@ -433,7 +464,14 @@ int aco_colony_initialize(aco_colony *c) {
 int aco_colony_construct_solution(aco_colony *c, float *timers_ms) {
   if (!c) return ACO_ERR_INVALID_ARGUMENT;
   if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
-  if (!timers_ms) return enqueue_iteration(c);
+  state_changed(c);
+  // Without timers one iteration is one replay of the captured graph (the
+  // legacy default stream cannot be captured: direct launches there).
+  if (!timers_ms) {
+    const bool capturable = c->stream != nullptr && c->stream != cudaStreamLegacy &&
+                            c->stream != cudaStreamPerThread;
+    return capturable ? aco_colony_run(c, 1) : enqueue_iteration(c);
+  }
   const ColonyDev d = make_dev(c);
   ACO_CUDA(c, cudaEventRecord(c->ev[0], c->stream), "event");
   ACO_CUDA(c, launch_construction(c, d), "construct");
@@ -444,10 +482,10 @@ int aco_colony_construct_solution(aco_colony *c, float *timers_ms) {
     ACO_CUDA(c, launch_evaporate(d, c->stream), "evaporate");
     ACO_CUDA(c, launch_deposit_atomic(d, c->stream), "deposit");
     ACO_CUDA(c, launch_pheromone_rows(d, false, false, false, c->stream), "choice rows");
-    c->launches += 5;
+    c->launches += 4 + construction_launches(c);
   } else {
     ACO_CUDA(c, launch_pheromone_rows(d, true, true, true, c->stream), "pheromone rows");
-    c->launches += 3;
+    c->launches += 2 + construction_launches(c);
   }
   ACO_CUDA(c, cudaEventRecord(c->ev[3], c->stream), "event");
   ACO_CUDA(c, cudaEventSynchronize(c->ev[3]), "synchronize");
@@ -464,6 +502,7 @@ int aco_colony_construct_solution(aco_colony *c, float *timers_ms) {
 
 int aco_colony_run(aco_colony *c, int32_t iterations) {
   if (!c || iterations < 0) return ACO_ERR_INVALID_ARGUMENT;
+  state_changed(c);
   if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
   if (iterations == 0) return ACO_OK;
   if (!c->graph_exec) {
@@ -481,7 +520,7 @@ int aco_colony_run(aco_colony *c, int32_t iterations) {
     ACO_CUDA(c, cudaGraphInstantiate(&c->graph_exec, g, 0), "instantiate");
     c->launches = before;  // capture itself launches nothing
   }
-  const int per_iter = c->p.deposit == ACO_DEPOSIT_ATOMIC ? 5 : 3;
+  const int per_iter = (c->p.deposit == ACO_DEPOSIT_ATOMIC ? 4 : 2) + construction_launches(c);
   for (int32_t i = 0; i < iterations; i++)
     ACO_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream), "graph launch");
   c->launches += (int64_t)per_iter * iterations;
@@ -614,6 +653,7 @@ int aco_colony_read_pheromone(aco_colony *c, float *out) {
 }
 
 int aco_colony_write_pheromone(aco_colony *c, const float *in) {
+  if (c) state_changed(c);
   if (!c || !in) return ACO_ERR_INVALID_ARGUMENT;
   if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
   ACO_CUDA(c, cudaMemcpy2DAsync(c->tau, (size_t)c->ld * 4, in, (size_t)c->n * 4, (size_t)c->n * 4,
@@ -746,6 +786,7 @@ void aco_colony_destroy(aco_colony *c) {
   for (int i = 0; i < 4; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  if (c->h_state) cudaFreeHost(c->h_state);
   delete c;
 }
 
@@ -863,6 +904,7 @@ int batch_build_items(aco_batch *b) {
 }
 
 int batch_enqueue(aco_batch *b, bool construct, bool epilogue, bool rows, bool update) {
+  for (aco_colony *c : b->cols) state_changed(c);
   if (construct) {
     ACO_BCUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream), "reset queue");
     ACO_BCUDA(b, launch_batch_construct(b->d_descs, b->d_items, b->num_items, b->d_queue, b->grid,
@@ -1055,6 +1097,7 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
   if (int s = batch_build_items(b)) return s;
   // The timing runs advanced ages and counters: back to the initialised state.
   for (aco_colony *c : b->cols) {
+    state_changed(c);
     const ColonyDev d = make_dev(c);
     ACO_BCUDA(b, launch_init_colony(d, b->stream), "reset");
     ACO_BCUDA(b, launch_pheromone_rows(d, false, false, false, b->stream), "reset rows");

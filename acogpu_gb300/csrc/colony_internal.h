@@ -29,6 +29,7 @@ struct aco_colony {
   float *mean = nullptr;
   int32_t *dep_col = nullptr;
   float *dep_delta = nullptr;
+  int32_t *plan = nullptr;  // aging colonies: the ants' roles of an iteration
   aco::ColonyState *st = nullptr;
   int16_t *nn16 = nullptr;  // candidate ids as int16, pitch ldk (k <= 32 kernels)
   float *xy = nullptr;      // coordinates (x then y) when created from coordinates
@@ -44,8 +45,17 @@ struct aco_colony {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // Host copy of the device state block (pinned), valid until the next call
+  // that enqueues work on the colony: the getters of one iteration share one
+  // device-to-host read.
+  aco::ColonyState *h_state = nullptr;
+  bool state_fresh = false;
   std::string err;
 };
+
+// Every call that enqueues work on a colony (or rewrites its state) marks the
+// cached state block stale.
+inline void state_changed(aco_colony *c) { c->state_fresh = false; }
 
 namespace aco {
 // Device view of a colony (pointers and parameters passed to the kernels).

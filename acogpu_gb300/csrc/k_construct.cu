@@ -535,6 +535,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
         if (hit != 0u) {  // a candidate id outside the instance: recorded, not used
           ok = false;
         } else if (c.fallback == ACO_FALLBACK_BEST) {
+          if (!BLEND && a.blend) a.meanc = smean[cur];  // pre-blended table
           next = fallback_best_reg(c, cur, tw, a, lane);
         } else {  // select_local_best on a full row of at most 32 cities (k == n)
           const unsigned um = __ballot_sync(kFull, id >= 0 && !vis);
@@ -560,30 +561,16 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
   return cur;
 }
 
-template <bool AGING, int TW, int G>
-__device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
-                                     const int16_t *sids, const float *scw, const float *smean,
-                                     int lane) {
+// The tour of one valid ant once its blend context is known: placement,
+// the step loop (BLEND: the aging fitness blend of every candidate per step;
+// otherwise the weights come blended, or plain, from the table), then the
+// integer length and the transposed successor/predecessor lists.
+template <int TW, int G, bool BLEND>
+__device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
+                                const int16_t *sids, const float *scw, const float *smean,
+                                AntCtx a, int lane) {
   const int n = c.n;
   int32_t *trow = c.tours + (size_t)k * c.ld;
-  AntCtx a;
-  a.blend = false;
-  a.ratio = 0.0f;
-  a.meanc = 0.0f;
-  if (AGING) {
-    int age = 0;
-    if (lane == 0) {
-      age = c.age[k] + 1;
-      c.age[k] = age;
-    }
-    age = __shfl_sync(kFull, age, 0);
-    if (!c.valid[k]) {  // invalid ants keep a cleared tour (src/Colony.cu:507-510)
-      for (int i = lane; i < n; i += 32) trow[i] = 0;
-      return;
-    }
-    a.blend = age < c.min_ret && c.st->isconverged;
-    if (a.blend) a.ratio = __fdiv_rn(__int2float_rn(age), __int2float_rn(c.min_ret));
-  }
   uint32_t tw[TW];
 #pragma unroll
   for (int t = 0; t < TW; t++) tw[t] = 0u;
@@ -598,10 +585,7 @@ __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, f
   reg_mark(tw, start, lane);
 
   int64_t fallbacks = 0;
-  if (AGING && a.blend)
-    staged_steps<TW, true, G>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
-  else
-    staged_steps<TW, false, G>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
+  staged_steps<TW, BLEND, G>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
   __syncwarp();
   // Tour length (order-free integer sum) and the transposed successor /
   // predecessor of every city for the row-owned deposit, one edge per lane.
@@ -626,6 +610,38 @@ __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, f
   }
 }
 
+// One ant with its aging step: updateAntAges (src/Colony.cu:353-364), the
+// cleared tour of an invalid ant (src/Colony.cu:507-510) and the blend
+// decision of compute_fittness (inc/Colony.cuh:21-30).
+template <bool AGING, int TW, int G>
+__device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
+                                     const int16_t *sids, const float *scw, const float *smean,
+                                     int lane) {
+  AntCtx a;
+  a.blend = false;
+  a.ratio = 0.0f;
+  a.meanc = 0.0f;
+  if (AGING) {
+    int age = 0;
+    if (lane == 0) {
+      age = c.age[k] + 1;
+      c.age[k] = age;
+    }
+    age = __shfl_sync(kFull, age, 0);
+    if (!c.valid[k]) {
+      int32_t *trow = c.tours + (size_t)k * c.ld;
+      for (int i = lane; i < c.n; i += 32) trow[i] = 0;
+      return;
+    }
+    a.blend = age < c.min_ret && c.st->isconverged;
+    if (a.blend) a.ratio = __fdiv_rn(__int2float_rn(age), __int2float_rn(c.min_ret));
+  }
+  if (AGING && a.blend)
+    staged_ant_body<TW, G, true>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+  else
+    staged_ant_body<TW, G, false>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+}
+
 template <bool MULTI, bool AGING>
 __global__ void __launch_bounds__(512) k_construct(ColonyDev c, int nchunks) {
   extern __shared__ __align__(16) uint32_t smem_construct[];
@@ -640,15 +656,77 @@ __global__ void __launch_bounds__(512) k_construct(ColonyDev c, int nchunks) {
                                      nullptr, nchunks, lane);
 }
 
+// Aging colonies, before the staged construction: updateAntAges
+// (src/Colony.cu:353-364) for every ant, then the roles of the iteration's
+// ants -- the valid ants that blend (age < min_ret once the colony has
+// converged, inc/Colony.cuh:21-30) and all the others, each list in index
+// order: plan = {B, blend ants[B], other ants[m - B]}.  One CTA, a block
+// scan over per-thread runs of consecutive ants.
+__global__ void __launch_bounds__(1024) k_aging_plan(ColonyDev c) {
+  __shared__ int s_warp[32];
+  __shared__ int s_total;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, T = blockDim.x;
+  const int m = c.m;
+  const bool conv = c.st->isconverged != 0;
+  const int per = (m + T - 1) / T;
+  const int lo = min(m, tid * per), hi = min(m, lo + per);
+  int nb = 0;
+  for (int k = lo; k < hi; k++) {
+    const int a = c.age[k] + 1;
+    c.age[k] = a;
+    nb += (c.valid[k] && a < c.min_ret && conv) ? 1 : 0;
+  }
+  int x = nb;  // inclusive scan within the warp
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < (T >> 5) ? s_warp[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, w, o);
+      if (lane >= o) w += y;
+    }
+    s_warp[lane] = w;
+    if (lane == 31) s_total = w;
+  }
+  __syncthreads();
+  const int B = s_total;
+  int bi = (warp ? s_warp[warp - 1] : 0) + x - nb;  // blend ants before `lo`
+  int oi = lo - bi;
+  for (int k = lo; k < hi; k++) {
+    if (c.valid[k] && c.age[k] < c.min_ret && conv)
+      c.plan[1 + bi++] = k;
+    else
+      c.plan[1 + B + oi++] = k;
+  }
+  if (tid == 0) c.plan[0] = B;
+}
+
+cudaError_t launch_aging_plan(const ColonyDev &c, cudaStream_t s) {
+  k_aging_plan<<<1, 1024, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
 // Shared-memory layout of the staged kernel: the table of staged_layout,
 // then per warp 32 f32, then the mbarrier.  G = pitch / 4.
+//
+// Without aging every CTA stages the table and its warps build tours.  With
+// aging the ants' roles come from k_aging_plan: CTA b < B takes blend ant b
+// (and b + grid, ...) -- it fills its table with that ant's blended weights
+// for every candidate of every row (the same blend_fitness as a per-step
+// blend, so the same bits) and runs the ant on them at the speed of a plain
+// ant; the remaining CTAs stage the plain table and share the other ants.
 template <bool AGING, int TW, int G>
 __global__ void __launch_bounds__(kStagedMaxWarps * 32)
     k_construct_staged(ColonyDev c, const int16_t *nn16) {
   extern __shared__ __align__(128) unsigned char smem_staged[];
+  constexpr int SP = 4 * G;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
   const int n = c.n;
-  const StagedLayout L = staged_layout(n, c.ld, 4 * G, AGING);
+  const StagedLayout L = staged_layout(n, c.ld, SP, AGING);
   float *scw = reinterpret_cast<float *>(smem_staged);
   int16_t *sids = reinterpret_cast<int16_t *>(smem_staged + L.ids_off);
   float *smean = reinterpret_cast<float *>(smem_staged + L.mean_off);
@@ -656,19 +734,28 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_staged + L.table + (size_t)warps * 128);
   __shared__ int flag;
 
+  const int grid = gridDim.x;
+  const int B = AGING ? c.plan[0] : 0;
+  const int base = B < grid ? B : 0;          // first CTA of the other ants
+  const int P = grid - base;                  // CTAs sharing them
+  const bool has_blend = AGING && (int)blockIdx.x < B;
+  const bool has_other = (int)blockIdx.x >= base;
+  const uint32_t cw_bytes = (uint32_t)L.ids_off;
+
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     fence_barrier_init();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const uint32_t cw_bytes = (uint32_t)L.ids_off, id_bytes = (uint32_t)(L.mean_off - L.ids_off);
+    const uint32_t id_bytes = (uint32_t)(L.mean_off - L.ids_off);
     const uint32_t mean_bytes = AGING ? (uint32_t)c.ld * 4u : 0u;
-    mbar_arrive_expect_tx(bar, cw_bytes + id_bytes + mean_bytes);
+    const uint32_t w_bytes = has_blend ? 0u : cw_bytes;  // a blend CTA fills its weights
+    mbar_arrive_expect_tx(bar, w_bytes + id_bytes + mean_bytes);
     constexpr uint32_t kPiece = 32768;
     const char *g = reinterpret_cast<const char *>(c.choice_nn);
-    for (uint32_t o = 0; o < cw_bytes; o += kPiece)
-      tma_load_1d(reinterpret_cast<char *>(scw) + o, g + o, min(kPiece, cw_bytes - o), bar);
+    for (uint32_t o = 0; o < w_bytes; o += kPiece)
+      tma_load_1d(reinterpret_cast<char *>(scw) + o, g + o, min(kPiece, w_bytes - o), bar);
     g = reinterpret_cast<const char *>(nn16);
     for (uint32_t o = 0; o < id_bytes; o += kPiece)
       tma_load_1d(reinterpret_cast<char *>(sids) + o, g + o, min(kPiece, id_bytes - o), bar);
@@ -678,8 +765,64 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
   __syncthreads();
   if (!flag) return;
   const uint32_t iter = c.st->iteration;
-  for (int k = blockIdx.x * warps + warp; k < c.m; k += gridDim.x * warps)
-    construct_ant_staged<AGING, TW, G>(c, k, iter, wbuf, sids, scw, smean, lane);
+
+  if (AGING && has_blend) {
+    for (int b = blockIdx.x; b < B; b += grid) {
+      const int k = c.plan[1 + b];
+      const float ratio = __fdiv_rn(__int2float_rn(c.age[k]), __int2float_rn(c.min_ret));
+      for (int t = threadIdx.x; t < n * SP; t += blockDim.x) {
+        const int j = t / SP, r = t - j * SP;
+        float w = 0.0f;
+        if (r < c.K) {
+          const size_t off = (size_t)j * c.ldk + r;
+          w = blend_fitness(c.tau_nn[off], __ldg(c.eta_nn + off), smean[j], ratio, c.use_alpha,
+                            c.alpha);
+        }
+        scw[t] = w;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        AntCtx a;
+        a.blend = true;
+        a.ratio = ratio;
+        a.meanc = 0.0f;
+        staged_ant_body<TW, G, false>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+      }
+      __syncthreads();
+    }
+    if (has_other) {  // more blend ants than CTAs: the plain weights back
+      if (threadIdx.x == 0) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, cw_bytes);
+        constexpr uint32_t kPiece = 32768;
+        const char *g = reinterpret_cast<const char *>(c.choice_nn);
+        for (uint32_t o = 0; o < cw_bytes; o += kPiece)
+          tma_load_1d(reinterpret_cast<char *>(scw) + o, g + o, min(kPiece, cw_bytes - o), bar);
+        flag = mbar_wait_bounded(bar, 1, c.st) ? 1 : 0;
+      }
+      __syncthreads();
+      if (!flag) return;
+    }
+  }
+  if (!has_other) return;
+  const int others = c.m - B;
+  for (int i = ((int)blockIdx.x - base) + P * warp; i < others; i += P * warps) {
+    if (!AGING) {
+      construct_ant_staged<false, TW, G>(c, i, iter, wbuf, sids, scw, smean, lane);
+      continue;
+    }
+    const int k = c.plan[1 + B + i];
+    if (!c.valid[k]) {  // invalid ants keep a cleared tour (src/Colony.cu:507-510)
+      int32_t *trow = c.tours + (size_t)k * c.ld;
+      for (int q = lane; q < n; q += 32) trow[q] = 0;
+      continue;
+    }
+    AntCtx a;
+    a.blend = false;
+    a.ratio = 0.0f;
+    a.meanc = 0.0f;
+    staged_ant_body<TW, G, false>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+  }
 }
 
 // k <= 32 with a candidate table too large for shared memory (e.g. n = 4096,

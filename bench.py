@@ -36,6 +36,10 @@ INSTANCE_SEED = 2026
 WORKLOAD = ("rank-based Ant System with aging, n=1000 (20 Gaussian clusters, sigma 300, "
             "[0,10000)^2), m=1000, w=6, k=30, rho=0.1")
 L2_FLUSH_BYTES = 256 << 20
+REF_BUDGET_S = 60.0  # CPU time the reference arm spends on its timed sample
+# Default timed steps per workload: about a second of timed work for the
+# single-colony lines (clock samples every 200 ms fall inside it).
+DEFAULT_STEPS = {"rbas_aging_n1000": 2000, "large4096": 300, "batch512": 10, "learned": 0}
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -172,22 +176,28 @@ def run_reference(args, rank):
     q.initialize()
     for _ in range(args.warmup):
         q.iterate()
-    tours = 0
+    # A bounded sample of the requested steps: about REF_BUDGET_S seconds of
+    # CPU work (the rate, not the count, is the result).
+    tours, done = 0, 0
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    while done < args.steps:
         q.iterate()
         tours += q.num_valid()
+        done += 1
+        if time.perf_counter() - t0 > REF_BUDGET_S:
+            break
     dt = time.perf_counter() - t0
     v = tours / dt
     return {"metric": "tours/s", "value": v, "unit": "tours/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": 1e3 * dt / done, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD + " -- reference CPU algorithm: full-row roulette "
                        "(no candidate lists), AS update (the reference's rank-based update is an "
                        "empty stub)", "n": N_CITIES, "m": N_ANTS, "k": N_CITIES},
             "cpu_baseline": {"value": v, "unit": "tours/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} iterations after {args.warmup} warm-up, "
+                             "sample": f"{done} of {args.steps} iterations (at most "
+                                       f"{REF_BUDGET_S:.0f} s) after {args.warmup} warm-up, "
                                        f"C restatement of the reference CPU path, {threads} "
                                        f"threads"},
             "e2e": {"value": v, "unit": "tours/s", "h2d_bytes_per_step": 0,
@@ -204,7 +214,9 @@ def run_ours(args, rank, world, local):
     p = workload_params()
     p.seed = 1234 + 7919 * rank  # independent replicas
 
-    stream = torch.cuda.current_stream(dev)
+    # The colony's own stream (not the legacy default stream, which cannot be
+    # captured): an iteration is one replay of the captured graph.
+    stream = torch.cuda.Stream(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     def barrier():
@@ -225,14 +237,13 @@ def run_ours(args, rank, world, local):
     stage = np.zeros(6)
     barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    with ClockSampler(local) as clk, torch.cuda.stream(stream):
         wall0 = time.perf_counter()
         for i in range(args.steps):
             flush.zero_()  # L2 flush, outside the timed events
             ev[i][0].record(stream)
-            t = col.constructSolution(timers=True)
+            col.constructSolution()
             ev[i][1].record(stream)
-            stage += t
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     barrier()
@@ -242,6 +253,14 @@ def run_ours(args, rank, world, local):
     launches = col.launch_count() - launches0
     tours = st1["tours_built"] - st0["tours_built"]
     fallbacks = st1["fallbacks"] - st0["fallbacks"]
+    # Stage breakdown: further iterations with per-stage events (outside the
+    # timed steps above), L2 flushed before each.
+    stage_steps = min(args.steps, 20)
+    with torch.cuda.stream(stream):
+        for _ in range(stage_steps):
+            flush.zero_()
+            stage += col.constructSolution(timers=True)
+    stage *= args.steps / max(1, stage_steps)
     col.close()
 
     # ---------------- end to end through the public API (host buffers)
@@ -547,7 +566,8 @@ def run_learned(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default per workload, see DEFAULT_STEPS)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -559,6 +579,8 @@ def main():
     ap.add_argument("--plain-iters", type=int, default=1000)
     ap.add_argument("--epochs", type=int, default=4)
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = DEFAULT_STEPS[args.workload]
     world, rank, local = dist_env()
     if args.impl == "reference":
         out = run_reference(args, rank)

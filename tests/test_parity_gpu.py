@@ -140,6 +140,22 @@ def test_construct_kernels_match_oracle(mode, aging):
     run_pair(p, d, 12 if aging else 5, ctx=f"mode{mode}")
 
 
+@pytest.mark.parametrize("m,six,iters", [
+    (120, (10, 12, 2, 100), 40),   # after convergence up to 10 blend ants per iteration
+    (400, (300, 5, 2, 390), 12),   # more blend ants than SMs: blend CTAs restage the table
+])
+def test_staged_blend_ants_match_oracle(m, six, iters):
+    """Aging colonies on the staged kernel: ants that blend run on a table of
+    their own blended weights (one CTA each), the others on the plain table;
+    tours, lengths, pheromone and ages stay bit-identical to the oracle."""
+    _, _, d = instance(200, 77, kind="clustered")
+    p = params(num_ants=m, beta=2.0, rho=0.2, cand_k=20, seed=77, aging=1,
+               construct_mode=_abi.ACO_CONSTRUCT_STAGED, **FAST_MODE)
+    (p.min_retirement_age, p.max_retirement_age, p.global_performance,
+     p.min_population_limit) = six
+    run_pair(p, d, iters, ctx=f"blend m{m}")
+
+
 @pytest.mark.parametrize("n,k,aging", [(1500, 32, 0), (3000, 20, 1), (5000, 32, 0)])
 def test_direct_kernel_matches_oracle(n, k, aging):
     """k <= 32 with a candidate table too large for shared memory: the step
