@@ -372,7 +372,9 @@ __device__ __forceinline__ uint32_t tw_pick(const uint32_t (&tw)[TW], int t) {
 // of n cities waits for ceil(n / 512) L2 round trips, not one per chunk.
 // Inlined: the tabu words must stay in registers (a call would take the
 // array's address and move it to local memory).
-template <int TW>
+// WIDE: the blend scan also issues its loads two chunks at a time (more
+// registers; used where the kernel has them to spare).
+template <int TW, bool WIDE>
 __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
                                                  const uint32_t (&tw)[TW], const AntCtx &a,
                                                  int lane) {
@@ -408,7 +410,42 @@ __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
         }
       }
     }
-  } else {  // aging blend (young ants after convergence): tau and eta rows
+  } else if (WIDE) {  // aging blend (young ants after convergence): tau and
+                      // eta rows, two 128-city chunks at a time
+#pragma unroll
+    for (int t0 = 0; t0 < 8 * TW; t0 += 2) {  // n <= 1024 * TW
+      if (t0 * 128 >= c.n) continue;
+      float4 tq[2], eq[2];
+#pragma unroll
+      for (int t = 0; t < 2; t++) {
+        const int j4 = (t0 + t) * 128 + lane * 4;
+        const bool in = j4 < c.n;
+        tq[t] = in ? __ldcg(reinterpret_cast<const float4 *>(trow + j4))
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+        eq[t] = in ? __ldg(reinterpret_cast<const float4 *>(erow + j4))
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int t = 0; t < 2; t++) {
+        const int j4 = (t0 + t) * 128 + lane * 4;
+        const uint32_t v =
+            __shfl_sync(kFull, tw_pick(tw, (t0 + t) >> 3), ((t0 + t) * 4 + (lane >> 3)) & 31);
+        const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
+        const float ta[4] = {tq[t].x, tq[t].y, tq[t].z, tq[t].w};
+        const float ea[4] = {eq[t].x, eq[t].y, eq[t].z, eq[t].w};
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          if (!((bits >> r) & 1u) && j4 + r < c.n) {
+            const float q = blend_fitness(ta[r], ea[r], a.meanc, a.ratio, c.use_alpha, c.alpha);
+            if (q > bw) {
+              bw = q;
+              bj = j4 + r;
+            }
+          }
+        }
+      }
+    }
+  } else {  // aging blend, one 128-city chunk per round trip
     for (int base = 0; base < c.n; base += 128) {
       const int j4 = base + lane * 4;
       const int word = j4 >> 5;  // register word >> 5 (uniform), lane word & 31
@@ -467,7 +504,7 @@ __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
 // uniforms of 32 consecutive steps are computed one per lane and broadcast;
 // the tour positions of the current 32-step block stay in one register per
 // lane and are stored together.
-template <int TW, bool BLEND, int G>
+template <int TW, bool BLEND, int G, bool WIDE = false>
 __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t akey, int start,
                                             uint32_t (&tw)[TW], float *wbuf, const int16_t *sids,
                                             const float *scw, const float *smean, AntCtx a,
@@ -536,7 +573,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
           ok = false;
         } else if (c.fallback == ACO_FALLBACK_BEST) {
           if (!BLEND && a.blend) a.meanc = smean[cur];  // pre-blended table
-          next = fallback_best_reg(c, cur, tw, a, lane);
+          next = fallback_best_reg<TW, WIDE>(c, cur, tw, a, lane);
         } else {  // select_local_best on a full row of at most 32 cities (k == n)
           const unsigned um = __ballot_sync(kFull, id >= 0 && !vis);
           next = um ? __shfl_sync(kFull, id, 31 - __clz(um)) : -1;
@@ -565,7 +602,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
 // the step loop (BLEND: the aging fitness blend of every candidate per step;
 // otherwise the weights come blended, or plain, from the table), then the
 // integer length and the transposed successor/predecessor lists.
-template <int TW, int G, bool BLEND>
+template <int TW, int G, bool BLEND, bool WIDE = false>
 __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
                                 const int16_t *sids, const float *scw, const float *smean,
                                 AntCtx a, int lane) {
@@ -585,7 +622,8 @@ __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float 
   reg_mark(tw, start, lane);
 
   int64_t fallbacks = 0;
-  staged_steps<TW, BLEND, G>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane, fallbacks);
+  staged_steps<TW, BLEND, G, WIDE>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane,
+                                   fallbacks);
   __syncwarp();
   // Tour length (order-free integer sum) and the transposed successor /
   // predecessor of every city for the row-owned deposit, one edge per lane.
@@ -770,15 +808,21 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
     for (int b = blockIdx.x; b < B; b += grid) {
       const int k = c.plan[1 + b];
       const float ratio = __fdiv_rn(__int2float_rn(c.age[k]), __int2float_rn(c.min_ret));
-      for (int t = threadIdx.x; t < n * SP; t += blockDim.x) {
-        const int j = t / SP, r = t - j * SP;
-        float w = 0.0f;
-        if (r < c.K) {
-          const size_t off = (size_t)j * c.ldk + r;
-          w = blend_fitness(c.tau_nn[off], __ldg(c.eta_nn + off), smean[j], ratio, c.use_alpha,
-                            c.alpha);
-        }
-        scw[t] = w;
+      // Rows of the candidate arrays are contiguous at pitch SP (a multiple
+      // of 4): four entries of one row per 16-byte load.
+      const float4 *tau4 = reinterpret_cast<const float4 *>(c.tau_nn);
+      const float4 *eta4 = reinterpret_cast<const float4 *>(c.eta_nn);
+      float4 *scw4 = reinterpret_cast<float4 *>(scw);
+      for (int t = threadIdx.x; t < n * G; t += blockDim.x) {
+        const int j = t / G, r0 = (t - j * G) * 4;
+        const float4 tv = tau4[t], ev = __ldg(eta4 + t);
+        const float mj = smean[j];
+        float4 w;
+        w.x = r0 + 0 < c.K ? blend_fitness(tv.x, ev.x, mj, ratio, c.use_alpha, c.alpha) : 0.0f;
+        w.y = r0 + 1 < c.K ? blend_fitness(tv.y, ev.y, mj, ratio, c.use_alpha, c.alpha) : 0.0f;
+        w.z = r0 + 2 < c.K ? blend_fitness(tv.z, ev.z, mj, ratio, c.use_alpha, c.alpha) : 0.0f;
+        w.w = r0 + 3 < c.K ? blend_fitness(tv.w, ev.w, mj, ratio, c.use_alpha, c.alpha) : 0.0f;
+        scw4[t] = w;
       }
       __syncthreads();
       if (warp == 0) {
@@ -786,7 +830,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
         a.blend = true;
         a.ratio = ratio;
         a.meanc = 0.0f;
-        staged_ant_body<TW, G, false>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+        staged_ant_body<TW, G, false, true>(c, k, iter, wbuf, sids, scw, smean, a, lane);
       }
       __syncthreads();
     }
