@@ -31,6 +31,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from acogpu_gb300 import distrib  # noqa: E402  (pure Python: no library load)
+
 N_CITIES, N_ANTS, RANK_W, CAND_K, RHO, BETA = 1000, 1000, 6, 30, 0.1, 2.0
 INSTANCE_SEED = 2026
 WORKLOAD = ("rank-based Ant System with aging, n=1000 (20 Gaussian clusters, sigma 300, "
@@ -212,7 +214,7 @@ def run_ours(args, rank, world, local):
     dev = torch.device("cuda", local)
     x, y, d = workload_instance()
     p = workload_params()
-    p.seed = 1234 + 7919 * rank  # independent replicas
+    p.seed = distrib.replica_seed(1234, rank)  # independent replicas
 
     # The colony's own stream (not the legacy default stream, which cannot be
     # captured): an iteration is one replay of the captured graph.
@@ -285,14 +287,9 @@ def run_ours(args, rank, world, local):
     barrier()
     e_tours = e_stats["tours_built"]
 
-    # max over ranks
-    vals = torch.tensor([dev_s, e_wall, wall], dtype=torch.float64, device=dev)
-    cnt = torch.tensor([tours, e_tours], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(vals, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(cnt, op=torch.distributed.ReduceOp.SUM)
-    dev_s, e_wall, wall = vals.tolist()
-    tours_all, e_tours_all = cnt.tolist()
+    # max over ranks of the times, sum of the work
+    (dev_s, e_wall, wall), (tours_all, e_tours_all) = distrib.reduce_times_and_counts(
+        [dev_s, e_wall, wall], [tours, e_tours], device=dev)
     if rank != 0:
         return None
 
@@ -355,13 +352,19 @@ def batch_params():
 
 
 def run_batch(args, rank, world, local):
-    """Batched uneven instances: whole-batch iterations, device-timed."""
+    """Batched uneven instances: whole-batch iterations, device-timed.  On N
+    GPUs, 512·N instances are generated and sharded by estimated cost (weak
+    scaling, no collective on the data path)."""
     import torch
     import acogpu_gb300 as aco
     torch.cuda.set_device(local)
-    insts = batch_instances()
+    allinst = batch_instances(BATCH_COUNT * world)
+    sizes_all = [len(x) for x, _ in allinst]
+    mine = distrib.shard_instances(sizes_all, np.minimum(sizes_all, BATCH_CAP), BATCH_K,
+                                   world)[rank]
+    insts = [allinst[i] for i in mine]
     p = batch_params()
-    p.seed = 4321 + 7919 * rank
+    p.seed = distrib.replica_seed(4321, rank)
     t0 = time.perf_counter()
     b = aco.Batch(insts, params=p, num_ants=BATCH_CAP)
     b.initialize()
@@ -381,22 +384,24 @@ def run_batch(args, rank, world, local):
     dev_s = start.elapsed_time(end) / 1e3
     tours = b.tours_built() - built0
     launches = b.launch_count() - launches0
-    sizes = np.array([len(x) for x, _ in insts])
+    sizes = np.array([len(x) for x, _ in allinst])
     ants = np.minimum(sizes, BATCH_CAP)
     best = b.glob_best()
     b.close()
+    (dev_s,), (tours, launches, best_sum) = distrib.reduce_times_and_counts(
+        [dev_s], [tours, launches, float(best.sum())], device=torch.device("cuda", local))
     if rank != 0:
         return None
     return {"metric": "tours/s", "value": tours / dev_s, "unit": "tours/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": BATCH_WORKLOAD, "instances": len(insts),
+            "config": {"workload": BATCH_WORKLOAD, "instances": len(allinst),
                        "cities_total": int(sizes.sum()), "ants_per_iteration": int(ants.sum()),
                        "l2": "working set 5+ GB, larger than L2"},
             "ant_steps_per_s": float((ants * (sizes - 1)).sum()) * args.steps / dev_s,
             "autotune": tune, "setup_s": setup_s, "gpu_launches": int(launches),
-            "mean_best_length": float(best.mean()), "clocks": clk.summary()}
+            "mean_best_length": best_sum / len(allinst), "clocks": clk.summary()}
 
 
 def run_large(args, rank, world, local):
