@@ -1014,6 +1014,7 @@ int aco_batch_initialize(aco_batch *b) {
 int aco_batch_run(aco_batch *b, int32_t iterations) {
   if (!b || iterations < 0) return ACO_ERR_INVALID_ARGUMENT;
   if (!b->initialized) return bfail(b, ACO_ERR_NOT_INITIALIZED, "batch not initialized");
+  for (aco_colony *c : b->cols) state_changed(c);  // the replays rewrite every state block
   if (!b->graph_exec) {
     const int64_t before = b->launches;
     ACO_BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");

@@ -103,4 +103,9 @@ def test_uneven_batch_properties():
         assert is_permutation_rows(t, n)
         assert np.array_equal(tour_lengths(d, t), v.tour_lengths())
     assert b.launch_count() - launches0 == 9  # three launches per batch iteration
+    built = b.tours_built()
+    b.run(2)  # graph replays only: the state read after them must be fresh
+    b.synchronize()
+    assert b.tours_built() - built == 2 * sum(min(n, 1024) for n in sizes)
+    assert np.all(b.glob_best() <= after)
     b.close()
