@@ -76,7 +76,7 @@ struct ColonyDev {
   float *mean;
   int32_t *dep_col;
   float *dep_delta;
-  int32_t *plan;  // aging, staged: {B, blend ants[B], other ants[m - B]} (m + 1)
+  int32_t *plan;  // aging, staged: {B, V, blend[B], valid others[V], invalid} (m + 2)
   ColonyState *st;
   float rho, alpha;
   int use_alpha;

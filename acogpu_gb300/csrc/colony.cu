@@ -130,7 +130,7 @@ int allocate(aco_colony *c) {
   if ((s = dalloc(c, &c->mean, ld))) return s;
   if (c->K <= 32 && c->n < 32768)
     if ((s = dalloc(c, &c->nn16, n * ldk))) return s;
-  if ((s = dalloc(c, &c->plan, m + 1))) return s;
+  if ((s = dalloc(c, &c->plan, m + 2))) return s;
   if ((s = dalloc(c, &c->dep_col, m + 1))) return s;
   if ((s = dalloc(c, &c->dep_delta, m + 1))) return s;
   if ((s = dalloc(c, &c->st, 1))) return s;
@@ -1071,6 +1071,9 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
       best_apb = apb;
     }
   }
+  // The row pass is timed as it runs in an iteration (evaporation and the
+  // deposit list of one epilogue); the instances are reset afterwards.
+  if (int s = batch_enqueue(b, false, true, false, false)) return s;
   const int threads[3] = {128, 256, 512};
   float best_rows = 1e30f;
   int best_threads = b->row_threads;
@@ -1079,7 +1082,7 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
     float ms = 1e30f;
     for (int rep = 0; rep < 2; rep++) {
       cudaEventRecord(e0, b->stream);
-      if (int s = batch_enqueue(b, false, false, true, false)) return s;
+      if (int s = batch_enqueue(b, false, false, true, true)) return s;
       cudaEventRecord(e1, b->stream);
       ACO_BCUDA(b, cudaEventSynchronize(e1), "tune rows");
       float v = 0;
@@ -1117,7 +1120,7 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
 
 int aco_batch_set_tuning(aco_batch *b, int32_t ants_per_block, int32_t row_threads) {
   if (!b || ants_per_block < 1 || ants_per_block > 16 ||
-      (row_threads != 0 && (row_threads < 32 || row_threads > 512 || row_threads % 32)))
+      (row_threads != 0 && (row_threads < 64 || row_threads > 512 || row_threads % 32)))
     return ACO_ERR_INVALID_ARGUMENT;
   b->apb = ants_per_block;
   if (row_threads) b->row_threads = row_threads;

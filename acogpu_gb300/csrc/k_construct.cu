@@ -626,8 +626,11 @@ __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float 
                                    fallbacks);
   __syncwarp();
   // Tour length (order-free integer sum) and the transposed successor /
-  // predecessor of every city for the row-owned deposit, one edge per lane.
+  // predecessor of every city for the row-owned deposit, one edge per lane;
+  // unrolled so a lane's distance reads (scattered, from HBM when the L2 is
+  // cold) are in flight together.
   int64_t len = 0;
+#pragma unroll 8
   for (int i = lane; i < n; i += 32) {
     const int a0 = trow[i];
     const int b0 = trow[i + 1 == n ? 0 : i + 1];
@@ -696,51 +699,76 @@ __global__ void __launch_bounds__(512) k_construct(ColonyDev c, int nchunks) {
 
 // Aging colonies, before the staged construction: updateAntAges
 // (src/Colony.cu:353-364) for every ant, then the roles of the iteration's
-// ants -- the valid ants that blend (age < min_ret once the colony has
-// converged, inc/Colony.cuh:21-30) and all the others, each list in index
-// order: plan = {B, blend ants[B], other ants[m - B]}.  One CTA, a block
-// scan over per-thread runs of consecutive ants.
-__global__ void __launch_bounds__(1024) k_aging_plan(ColonyDev c) {
-  __shared__ int s_warp[32];
-  __shared__ int s_total;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, T = blockDim.x;
-  const int m = c.m;
-  const bool conv = c.st->isconverged != 0;
-  const int per = (m + T - 1) / T;
-  const int lo = min(m, tid * per), hi = min(m, lo + per);
-  int nb = 0;
-  for (int k = lo; k < hi; k++) {
-    const int a = c.age[k] + 1;
-    c.age[k] = a;
-    nb += (c.valid[k] && a < c.min_ret && conv) ? 1 : 0;
-  }
-  int x = nb;  // inclusive scan within the warp
+// ants, each list in index order: the valid ants that blend (age < min_ret
+// once the colony has converged, inc/Colony.cuh:21-30), the other valid
+// ants, the invalid ants (a cleared tour each).  plan = {B, V, blend[B],
+// valid others[V], invalid[m - B - V]}; the valid ones come first so that the
+// staged kernel spreads them evenly.  One CTA, block scans over per-thread
+// runs of consecutive ants.
+__device__ __forceinline__ int2 block_exclusive_scan2(int2 v, int2 *s_warp, int2 *s_total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int2 x = v;  // inclusive within the warp
   for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(kFull, x, o);
-    if (lane >= o) x += y;
+    const int yx = __shfl_up_sync(kFull, x.x, o), yy = __shfl_up_sync(kFull, x.y, o);
+    if (lane >= o) {
+      x.x += yx;
+      x.y += yy;
+    }
   }
   if (lane == 31) s_warp[warp] = x;
   __syncthreads();
   if (warp == 0) {
-    int w = lane < (T >> 5) ? s_warp[lane] : 0;
+    int2 w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : make_int2(0, 0);
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(kFull, w, o);
-      if (lane >= o) w += y;
+      const int yx = __shfl_up_sync(kFull, w.x, o), yy = __shfl_up_sync(kFull, w.y, o);
+      if (lane >= o) {
+        w.x += yx;
+        w.y += yy;
+      }
     }
     s_warp[lane] = w;
-    if (lane == 31) s_total = w;
+    if (lane == 31) *s_total = w;
   }
   __syncthreads();
-  const int B = s_total;
-  int bi = (warp ? s_warp[warp - 1] : 0) + x - nb;  // blend ants before `lo`
-  int oi = lo - bi;
+  const int2 before = warp ? s_warp[warp - 1] : make_int2(0, 0);
+  return make_int2(before.x + x.x - v.x, before.y + x.y - v.y);
+}
+
+__global__ void __launch_bounds__(1024) k_aging_plan(ColonyDev c) {
+  __shared__ int2 s_warp[32];
+  __shared__ int2 s_total;
+  const int tid = threadIdx.x, T = blockDim.x;
+  const int m = c.m;
+  const bool conv = c.st->isconverged != 0;
+  const int per = (m + T - 1) / T;
+  const int lo = min(m, tid * per), hi = min(m, lo + per);
+  int2 cnt = make_int2(0, 0);  // (blend, valid other) in [lo, hi)
   for (int k = lo; k < hi; k++) {
-    if (c.valid[k] && c.age[k] < c.min_ret && conv)
-      c.plan[1 + bi++] = k;
-    else
-      c.plan[1 + B + oi++] = k;
+    const int a = c.age[k] + 1;
+    c.age[k] = a;
+    if (c.valid[k]) {
+      if (a < c.min_ret && conv)
+        cnt.x++;
+      else
+        cnt.y++;
+    }
   }
-  if (tid == 0) c.plan[0] = B;
+  const int2 off = block_exclusive_scan2(cnt, s_warp, &s_total);
+  const int B = s_total.x, V = s_total.y;
+  int bi = off.x, vi = off.y, ii = lo - off.x - off.y;
+  int32_t *list = c.plan + 2;
+  for (int k = lo; k < hi; k++) {
+    if (!c.valid[k])
+      list[B + V + ii++] = k;
+    else if (c.age[k] < c.min_ret && conv)
+      list[bi++] = k;
+    else
+      list[B + vi++] = k;
+  }
+  if (tid == 0) {
+    c.plan[0] = B;
+    c.plan[1] = V;
+  }
 }
 
 cudaError_t launch_aging_plan(const ColonyDev &c, cudaStream_t s) {
@@ -774,6 +802,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
 
   const int grid = gridDim.x;
   const int B = AGING ? c.plan[0] : 0;
+  const int32_t *plan_list = c.plan + 2;
   const int base = B < grid ? B : 0;          // first CTA of the other ants
   const int P = grid - base;                  // CTAs sharing them
   const bool has_blend = AGING && (int)blockIdx.x < B;
@@ -806,7 +835,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
 
   if (AGING && has_blend) {
     for (int b = blockIdx.x; b < B; b += grid) {
-      const int k = c.plan[1 + b];
+      const int k = plan_list[b];
       const float ratio = __fdiv_rn(__int2float_rn(c.age[k]), __int2float_rn(c.min_ret));
       // Rows of the candidate arrays are contiguous at pitch SP (a multiple
       // of 4): four entries of one row per 16-byte load.
@@ -855,7 +884,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
       construct_ant_staged<false, TW, G>(c, i, iter, wbuf, sids, scw, smean, lane);
       continue;
     }
-    const int k = c.plan[1 + B + i];
+    const int k = plan_list[B + i];
     if (!c.valid[k]) {  // invalid ants keep a cleared tour (src/Colony.cu:507-510)
       int32_t *trow = c.tours + (size_t)k * c.ld;
       for (int q = lane; q < n; q += 32) trow[q] = 0;

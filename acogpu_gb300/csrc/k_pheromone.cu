@@ -28,6 +28,10 @@
 namespace aco {
 
 constexpr int kRowThreads = 256;
+// Deposit entries staged per segment (double-buffered: warps 1.. load the
+// next segment's successor, predecessor and delta while warp 0 folds this
+// one), so the ordered fold reads shared memory only.
+constexpr int kDepSeg = 256;
 
 __device__ __forceinline__ float choice_of(float tau, float eta, int use_alpha, float alpha) {
   const float p = use_alpha ? powf(tau, alpha) : tau;
@@ -41,7 +45,10 @@ __device__ __forceinline__ void pheromone_row_body(const ColonyDev &c, const int
   float *row = reinterpret_cast<float *>(smem_rows);
   float *erow = row + ld;
   uint32_t *mt = reinterpret_cast<uint32_t *>(erow + ld);
-  float *dl = reinterpret_cast<float *>(mt + (DEPOSIT ? ld : 0));
+  int *seg_s = reinterpret_cast<int *>(mt + (DEPOSIT ? ld : 0));  // [2][kDepSeg]
+  int *seg_p = seg_s + (DEPOSIT ? 2 * kDepSeg : 0);
+  float *seg_d = reinterpret_cast<float *>(seg_p + (DEPOSIT ? 2 * kDepSeg : 0));
+  float *dl = seg_d + (DEPOSIT ? 2 * kDepSeg : 0);
   uint64_t *bar = reinterpret_cast<uint64_t *>(dl + 32);
   int *flag = reinterpret_cast<int *>(bar + 1);
 
@@ -73,62 +80,78 @@ __device__ __forceinline__ void pheromone_row_body(const ColonyDev &c, const int
   }
 
   if (DEPOSIT) {
-    if (tid < 32) {
-      const int lane = tid;
-      const int cnt = c.st->dep_count;
-      const size_t base_row = (size_t)j * c.ldm;
-      for (int base = 0; base < cnt; base += 32) {
-        const int q = base + lane;
-        int col = -1;
-        float d = 0.0f;
-        if (q < cnt) {
-          col = c.dep_col[q];
-          d = c.dep_delta[q];
-        }
+    const int cnt = c.st->dep_count;
+    const size_t base_row = (size_t)j * c.ldm;
+    // Segment `seg` of the deposit list -> buffer `buf`: for each entry the
+    // successor and predecessor of city j in that ant's tour and its delta.
+    auto stage = [&](int seg, int buf) {
+      for (int q = tid - 32; q < kDepSeg; q += nthreads - 32) {
+        const int e = seg * kDepSeg + q;
         int sN = -1, pN = -1;
-        if (col >= 0) {
-          sN = c.succT[base_row + col];
-          pN = c.predT[base_row + col];
-          if ((unsigned)sN >= (unsigned)n || (unsigned)pN >= (unsigned)n) {
-            atomicOr(&c.st->error, kErrCheck);
-            sN = pN = -1;
-          }
-        }
-        dl[lane] = d;
-        if (sN >= 0) atomicOr(&mt[sN], 1u << lane);
-        if (pN >= 0) atomicOr(&mt[pN], 1u << lane);
-        __syncwarp();
-        if (sN >= 0) {
-          unsigned M = mt[sN];
-          if (__ffs(M) - 1 == lane) {
-            float v = row[sN];
-            while (M) {
-              const int b = __ffs(M) - 1;
-              M &= M - 1;
-              v = __fadd_rn(v, dl[b]);
+        float d = 0.0f;
+        if (e < cnt) {
+          const int col = c.dep_col[e];
+          d = c.dep_delta[e];
+          if (col >= 0) {
+            sN = c.succT[base_row + col];
+            pN = c.predT[base_row + col];
+            if ((unsigned)sN >= (unsigned)n || (unsigned)pN >= (unsigned)n) {
+              atomicOr(&c.st->error, kErrCheck);
+              sN = pN = -1;
             }
-            row[sN] = v;
           }
         }
-        if (pN >= 0) {
-          unsigned M = mt[pN];
-          if (__ffs(M) - 1 == lane) {
-            float v = row[pN];
-            while (M) {
-              const int b = __ffs(M) - 1;
-              M &= M - 1;
-              v = __fadd_rn(v, dl[b]);
-            }
-            row[pN] = v;
-          }
-        }
-        __syncwarp();
-        if (sN >= 0) mt[sN] = 0;
-        if (pN >= 0) mt[pN] = 0;
-        __syncwarp();
+        seg_s[buf * kDepSeg + q] = sN;
+        seg_p[buf * kDepSeg + q] = pN;
+        seg_d[buf * kDepSeg + q] = d;
       }
-    }
+    };
+    if (tid >= 32) stage(0, 0);
     __syncthreads();
+    for (int seg = 0; seg * kDepSeg < cnt; seg++) {
+      const int buf = seg & 1;
+      if (tid >= 32) {
+        if ((seg + 1) * kDepSeg < cnt) stage(seg + 1, buf ^ 1);
+      } else {
+        const int lane = tid;
+        const int end = min(kDepSeg, cnt - seg * kDepSeg);
+        for (int base = 0; base < end; base += 32) {
+          const int q = buf * kDepSeg + base + lane;
+          const bool in = base + lane < end;
+          const int sN = in ? seg_s[q] : -1, pN = in ? seg_p[q] : -1;
+          dl[lane] = in ? seg_d[q] : 0.0f;
+          if (sN >= 0) atomicOr(&mt[sN], 1u << lane);
+          if (pN >= 0) atomicOr(&mt[pN], 1u << lane);
+          __syncwarp();
+          // The lowest lane touching an element leads it and adds the deltas
+          // of every lane in its group, in lane (= ant) order: 32 unrolled
+          // predicated adds from broadcast registers, the successor and the
+          // predecessor element of a lane as two independent chains.
+          const unsigned Ms = sN >= 0 ? mt[sN] : 0u, Mp = pN >= 0 ? mt[pN] : 0u;
+          const unsigned As = (sN >= 0 && __ffs(Ms) - 1 == lane) ? Ms : 0u;
+          const unsigned Ap = (pN >= 0 && __ffs(Mp) - 1 == lane) ? Mp : 0u;
+          float vs = As ? row[sN] : 0.0f, vp = Ap ? row[pN] : 0.0f;
+          const float4 *dl4 = reinterpret_cast<const float4 *>(dl);
+#pragma unroll
+          for (int g = 0; g < 8; g++) {
+            const float4 q4 = dl4[g];
+            const float dq[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+              if ((As >> (4 * g + e)) & 1u) vs = __fadd_rn(vs, dq[e]);
+              if ((Ap >> (4 * g + e)) & 1u) vp = __fadd_rn(vp, dq[e]);
+            }
+          }
+          if (As) row[sN] = vs;
+          if (Ap) row[pN] = vp;
+          __syncwarp();
+          if (sN >= 0) mt[sN] = 0;
+          if (pN >= 0) mt[pN] = 0;
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+    }
   }
 
   float *trow = c.tau + (size_t)j * ld;
@@ -178,10 +201,11 @@ __global__ void __launch_bounds__(512) k_batch_pheromone_rows(const ColonyDev *d
 }
 
 static size_t rows_smem(int ld, bool deposit) {
-  return (size_t)ld * 4 * (deposit ? 3 : 2) + 32 * 4 + 16;
+  return (size_t)ld * 4 * (deposit ? 3 : 2) + (deposit ? 2 * kDepSeg * 12 : 0) + 32 * 4 + 16;
 }
 
-static int row_threads(int threads) { return threads > 0 ? threads : kRowThreads; }
+// At least two warps: warp 0 folds the deposits, the others stage them.
+static int row_threads(int threads) { return threads >= 64 ? threads : kRowThreads; }
 
 template <bool EVAP, bool DEPOSIT, bool WRITE_TAU>
 static cudaError_t launch_rows_t(const ColonyDev &c, int threads, cudaStream_t s) {

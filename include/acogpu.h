@@ -299,6 +299,8 @@ ACO_API int aco_batch_synchronize(aco_batch *b);
  * memory (about n <= 1150) are staged there, per work item, unless the batch
  * parameters ask for ACO_CONSTRUCT_GLOBAL; the others read rows from L2. */
 ACO_API int aco_batch_autotune(aco_batch *b, aco_tuning *out);
+/* ants_per_block 1..16; row_threads 0 (keep) or 64..512 in steps of 32 (warp
+ * 0 folds the deposits in order, the other warps stage them). */
 ACO_API int aco_batch_set_tuning(aco_batch *b, int32_t ants_per_block, int32_t row_threads);
 ACO_API int aco_batch_get_size(aco_batch *b, int32_t *count);
 /* Borrowed handle of instance i (read its state with the colony getters;
