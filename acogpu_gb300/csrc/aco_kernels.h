@@ -67,6 +67,11 @@ cudaError_t launch_aging_plan(const ColonyDev &c, cudaStream_t s);
 // k <= 32, rows read from L2 by the staged step loop (n <= kDirectMaxCities).
 constexpr int kDirectMaxCities = 8192;
 cudaError_t launch_construct_direct(const ColonyDev &c, int grid, int warps, cudaStream_t s);
+// k <= 32, the table split over a cluster of cs = ceil(n / 1024) CTAs (cs <= 8)
+// read through DSMEM.  The query gives how many such clusters fit at once.
+cudaError_t query_construct_cluster(const ColonyDev &c, int warps, int cs, int *max_clusters);
+cudaError_t launch_construct_cluster(const ColonyDev &c, int grid, int warps, int cs,
+                                     cudaStream_t s);
 cudaError_t launch_nn_to_i16(const int32_t *nn, int n, int ldk, int16_t *nn16, cudaStream_t s);
 cudaError_t launch_epilogue(const ColonyDev &c, cudaStream_t s);
 

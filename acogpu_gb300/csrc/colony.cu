@@ -100,9 +100,12 @@ int check_params(const aco_params *p, int n) {
   if (p->nn_order == ACO_NN_STABLE && n > 16384) return ACO_ERR_UNSUPPORTED;
   if (p->variant == ACO_RANK_BASED && p->rank_w < 1) return ACO_ERR_INVALID_ARGUMENT;
   if (p->ants_per_block < 0 || p->ants_per_block > 16) return ACO_ERR_INVALID_ARGUMENT;
-  if (p->construct_mode < ACO_CONSTRUCT_AUTO || p->construct_mode > ACO_CONSTRUCT_STAGED)
+  if (p->construct_mode < ACO_CONSTRUCT_AUTO || p->construct_mode > ACO_CONSTRUCT_CLUSTER)
     return ACO_ERR_INVALID_ARGUMENT;
   if (p->construct_mode == ACO_CONSTRUCT_STAGED && (K > 32 || n > 2048))
+    return ACO_ERR_UNSUPPORTED;
+  if ((p->construct_mode == ACO_CONSTRUCT_DIRECT || p->construct_mode == ACO_CONSTRUCT_CLUSTER) &&
+      (K > 32 || n > kDirectMaxCities))
     return ACO_ERR_UNSUPPORTED;
   return ACO_OK;
 }
@@ -128,8 +131,8 @@ int allocate(aco_colony *c) {
   if ((s = dalloc(c, &c->perf, m))) return s;
   if ((s = dalloc(c, &c->valid, m))) return s;
   if ((s = dalloc(c, &c->mean, ld))) return s;
-  if (c->K <= 32 && c->n < 32768)
-    if ((s = dalloc(c, &c->nn16, n * ldk))) return s;
+  // 16 bytes of slack: the cluster kernel stages slices in 16-byte units
+  if (c->K <= 32 && c->n < 32768 && (s = dalloc(c, &c->nn16, n * ldk + 8))) return s;
   if ((s = dalloc(c, &c->plan, m + 2))) return s;
   if ((s = dalloc(c, &c->dep_col, m + 1))) return s;
   if ((s = dalloc(c, &c->dep_delta, m + 1))) return s;
@@ -222,19 +225,24 @@ cudaError_t launch_construction(aco_colony *c, const ColonyDev &d) {
     }
     return launch_construct_staged(d, c->nn16, c->staged_grid, c->staged_warps, c->stream);
   }
+  if (c->cluster)
+    return launch_construct_cluster(d, c->staged_grid, c->staged_warps, c->cluster, c->stream);
   if (c->direct) return launch_construct_direct(d, c->staged_grid, c->staged_warps, c->stream);
   return launch_construct(d, c->apb, c->stream);
 }
 
 // Chooses the construction kernel, for k <= 32: the staged kernel (whole
 // candidate table in shared memory, one CTA per SM) when the table fits, else
-// the direct kernel (the same step loop on rows read from L2, n <= 8192);
-// otherwise, and in ACO_CONSTRUCT_GLOBAL mode, the general global-memory
-// kernel.  The first two put one ant per warp, ceil(m / SMs) warps per CTA.
+// the cluster kernel (the table split over ceil(n/1024) CTAs, n <= 8192),
+// else the direct kernel (the same step loop on rows read from L2); otherwise,
+// and in ACO_CONSTRUCT_GLOBAL mode, the general global-memory kernel.  The
+// k <= 32 kernels put one ant per warp.
 int plan_construction(aco_colony *c) {
   c->staged = false;
   c->direct = false;
-  if (c->K > 32 || !c->nn16 || c->p.construct_mode == ACO_CONSTRUCT_GLOBAL) return ACO_OK;
+  c->cluster = 0;
+  const int mode = c->p.construct_mode;
+  if (c->K > 32 || !c->nn16 || mode == ACO_CONSTRUCT_GLOBAL) return ACO_OK;
   const int sms = c->num_sms > 0 ? c->num_sms : 1;
   int warps = (c->m + sms - 1) / sms;
   warps = warps < 1 ? 1 : (warps > kStagedMaxWarps ? kStagedMaxWarps : warps);
@@ -252,7 +260,7 @@ int plan_construction(aco_colony *c) {
     c->staged_warps = warps < 1 ? 1 : (warps > kStagedMaxWarps ? kStagedMaxWarps : warps);
     c->staged_grid = sms;
   }
-  if (c->n <= 2048) {
+  if (c->n <= 2048 && (mode == ACO_CONSTRUCT_AUTO || mode == ACO_CONSTRUCT_STAGED)) {
     const size_t smem =
         construct_staged_smem_bytes(c->n, c->ld, c->ldk, c->p.aging != 0, c->staged_warps);
     if (smem <= (size_t)c->max_smem_optin) {
@@ -260,10 +268,35 @@ int plan_construction(aco_colony *c) {
       c->staged = true;
       return ACO_OK;
     }
-    if (c->p.construct_mode == ACO_CONSTRUCT_STAGED)
+    if (mode == ACO_CONSTRUCT_STAGED)
       return fail(c, ACO_ERR_UNSUPPORTED, "candidate table does not fit in shared memory");
   }
-  c->direct = c->n <= kDirectMaxCities;
+  if (c->n > kDirectMaxCities) return ACO_OK;
+  if (mode == ACO_CONSTRUCT_AUTO || mode == ACO_CONSTRUCT_CLUSTER) {
+    const int cs = (c->n + 1023) / 1024;
+    int clusters = 0;
+    const ColonyDev d = make_dev(c);
+    if (cs >= 2 && cs <= 8) {
+      // warps per CTA for the ants over the CTAs that fit, one pass
+      int w = (c->m + sms - 1) / sms;
+      w = w < 1 ? 1 : (w > kStagedMaxWarps ? kStagedMaxWarps : w);
+      if (query_construct_cluster(d, w, cs, &clusters) == cudaSuccess && clusters > 0) {
+        int ctas = clusters * cs;
+        w = (c->m + ctas - 1) / ctas;
+        w = w < 1 ? 1 : (w > kStagedMaxWarps ? kStagedMaxWarps : w);
+        const int need = (c->m + w - 1) / w;  // CTAs that get ants
+        ctas = std::min(ctas, (need + cs - 1) / cs * cs);
+        c->cluster = cs;
+        c->staged_warps = w;
+        c->staged_grid = ctas;
+        return ACO_OK;
+      }
+    }
+    cudaGetLastError();  // a refused query leaves no error behind
+    if (mode == ACO_CONSTRUCT_CLUSTER)
+      return fail(c, ACO_ERR_UNSUPPORTED, "no cluster of the needed size fits");
+  }
+  c->direct = true;
   return ACO_OK;
 }
 

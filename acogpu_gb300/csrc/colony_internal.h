@@ -35,6 +35,7 @@ struct aco_colony {
   float *xy = nullptr;      // coordinates (x then y) when created from coordinates
   bool staged = false;      // construction by the staged kernel
   bool direct = false;      // construction by the direct (L2-row) kernel
+  int cluster = 0;          // construction by the cluster kernel: CTAs per cluster
   int staged_grid = 0, staged_warps = 0;
   int num_sms = 0, max_smem_optin = 0;
   std::vector<void *> allocations;

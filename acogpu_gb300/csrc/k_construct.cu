@@ -349,12 +349,12 @@ template <int TW>
 __device__ __forceinline__ void reg_mark(uint32_t (&tw)[TW], int city, int lane) {
   const int word = city >> 5;
   const uint32_t bit = lane == (word & 31) ? 1u << (city & 31) : 0u;
-  if (TW == 1) {  // every city is below 1024
+  if constexpr (TW == 1) {  // every city is below 1024
     tw[0] |= bit;
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int t = 0; t < TW; t++) tw[t] |= (word >> 5) == t ? bit : 0u;
+    for (int t = 0; t < TW; t++) tw[t] |= (word >> 5) == t ? bit : 0u;
+  }
 }
 
 // Register t of the tabu words, t uniform across the warp (a select chain,
@@ -479,6 +479,53 @@ __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
   return bj;
 }
 
+// Where the step loop reads the candidate rows (pitch SP): a whole table in
+// shared or global memory, or -- in a thread-block cluster -- the slice of
+// the CTA that owns the row (rows r*1024 .. r*1024+1023 in cluster rank r,
+// at the same shared-memory offsets in every CTA), through DSMEM.
+template <int SP>
+struct TableRows {
+  const int16_t *ids;
+  const float *w;
+  const float *mean;
+  __device__ __forceinline__ int id(int cur, int lr) const { return ids[cur * SP + lr]; }
+  __device__ __forceinline__ float weight(int cur, int lr) const { return w[cur * SP + lr]; }
+  __device__ __forceinline__ float row_mean(int cur) const { return mean[cur]; }
+};
+
+constexpr int kClusterRows = 1024;  // rows in each CTA's slice
+
+template <int SP>
+struct ClusterRows {
+  uint32_t ids, w, mean;  // shared::cta addresses of the slice arrays
+  __device__ __forceinline__ static uint32_t owner_addr(uint32_t local, int cur) {
+    uint32_t r;
+    asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(cur >> 10));
+    return r;
+  }
+  __device__ __forceinline__ int id(int cur, int lr) const {
+    short v;
+    asm("ld.shared::cluster.s16 %0, [%1];"
+        : "=h"(v)
+        : "r"(owner_addr(ids + (uint32_t)((cur & (kClusterRows - 1)) * SP + lr) * 2u, cur)));
+    return v;
+  }
+  __device__ __forceinline__ float weight(int cur, int lr) const {
+    float v;
+    asm("ld.shared::cluster.f32 %0, [%1];"
+        : "=f"(v)
+        : "r"(owner_addr(w + (uint32_t)((cur & (kClusterRows - 1)) * SP + lr) * 4u, cur)));
+    return v;
+  }
+  __device__ __forceinline__ float row_mean(int cur) const {
+    float v;
+    asm("ld.shared::cluster.f32 %0, [%1];"
+        : "=f"(v)
+        : "r"(owner_addr(mean + (uint32_t)(cur & (kClusterRows - 1)) * 4u, cur)));
+    return v;
+  }
+};
+
 // The step loop of one ant; BLEND (the aging fitness blend, fixed for the
 // ant's whole tour) is a template parameter so the loop carries no per-step
 // test of it.  Rows of the staged table are padded to 32 entries with id -1
@@ -504,11 +551,10 @@ __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
 // uniforms of 32 consecutive steps are computed one per lane and broadcast;
 // the tour positions of the current 32-step block stay in one register per
 // lane and are stored together.
-template <int TW, bool BLEND, int G, bool WIDE = false>
+template <int TW, bool BLEND, int G, bool WIDE, class ROWS>
 __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t akey, int start,
-                                            uint32_t (&tw)[TW], float *wbuf, const int16_t *sids,
-                                            const float *scw, const float *smean, AntCtx a,
-                                            int lane, int64_t &fallbacks) {
+                                            uint32_t (&tw)[TW], float *wbuf, const ROWS &rows,
+                                            AntCtx a, int lane, int64_t &fallbacks) {
   constexpr int SP = 4 * G;  // row pitch of the staged table
   const int n = c.n;
   int32_t *trow = c.tours + (size_t)k * c.ld;
@@ -520,8 +566,8 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
   // sum, so they are never the first crossing.
   const int lr = lane < SP ? lane : SP - 1;
   int cur = start;
-  int id = sids[cur * SP + lr];
-  float wraw = BLEND ? 0.0f : scw[cur * SP + lr];
+  int id = rows.id(cur, lr);
+  float wraw = BLEND ? 0.0f : rows.weight(cur, lr);
   bool ok = true;
   for (int xb = 0; xb < n && ok; xb += 32) {
     const float ublk = aco_uniform_key(akey, (uint32_t)(xb + lane));
@@ -532,7 +578,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
       const float u = __shfl_sync(kFull, ublk, x & 31);
       float w = wraw;
       if (BLEND) {
-        a.meanc = smean[cur];  // every lane: the fallback scan uses it too
+        a.meanc = rows.row_mean(cur);  // every lane: the fallback scan uses it too
         const size_t off = (size_t)cur * c.ldk + lane;
         w = lane < c.K ? blend_fitness(c.tau_nn[off], __ldg(c.eta_nn + off), a.meanc, a.ratio,
                                        c.use_alpha, c.alpha)
@@ -566,13 +612,13 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
       // stand-in keeps the loads inside the table) and reloaded if the
       // fallback picks the city.
       const int nx = (unsigned)next < (unsigned)n ? next : 0;
-      int id_next = sids[nx * SP + lr];
-      float w_next = BLEND ? 0.0f : scw[nx * SP + lr];
+      int id_next = rows.id(nx, lr);
+      float w_next = BLEND ? 0.0f : rows.weight(nx, lr);
       if (hit == 0u || (unsigned)next >= (unsigned)n) {
         if (hit != 0u) {  // a candidate id outside the instance: recorded, not used
           ok = false;
         } else if (c.fallback == ACO_FALLBACK_BEST) {
-          if (!BLEND && a.blend) a.meanc = smean[cur];  // pre-blended table
+          if (!BLEND && a.blend) a.meanc = rows.row_mean(cur);  // pre-blended table
           next = fallback_best_reg<TW, WIDE>(c, cur, tw, a, lane);
         } else {  // select_local_best on a full row of at most 32 cities (k == n)
           const unsigned um = __ballot_sync(kFull, id >= 0 && !vis);
@@ -584,8 +630,8 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
           if (lane == 0) atomicOr(&c.st->error, kErrCheck);
           break;
         }
-        id_next = sids[next * SP + lr];
-        w_next = BLEND ? 0.0f : scw[next * SP + lr];
+        id_next = rows.id(next, lr);
+        w_next = BLEND ? 0.0f : rows.weight(next, lr);
       }
       reg_mark(tw, next, lane);
       tpos = lane == (x & 31) ? next : tpos;
@@ -602,10 +648,9 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
 // the step loop (BLEND: the aging fitness blend of every candidate per step;
 // otherwise the weights come blended, or plain, from the table), then the
 // integer length and the transposed successor/predecessor lists.
-template <int TW, int G, bool BLEND, bool WIDE = false>
+template <int TW, int G, bool BLEND, bool WIDE, class ROWS>
 __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
-                                const int16_t *sids, const float *scw, const float *smean,
-                                AntCtx a, int lane) {
+                                const ROWS &rows, AntCtx a, int lane) {
   const int n = c.n;
   int32_t *trow = c.tours + (size_t)k * c.ld;
   uint32_t tw[TW];
@@ -622,8 +667,7 @@ __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float 
   reg_mark(tw, start, lane);
 
   int64_t fallbacks = 0;
-  staged_steps<TW, BLEND, G, WIDE>(c, k, akey, start, tw, wbuf, sids, scw, smean, a, lane,
-                                   fallbacks);
+  staged_steps<TW, BLEND, G, WIDE>(c, k, akey, start, tw, wbuf, rows, a, lane, fallbacks);
   __syncwarp();
   // Tour length (order-free integer sum) and the transposed successor /
   // predecessor of every city for the row-owned deposit, one edge per lane;
@@ -654,10 +698,9 @@ __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float 
 // One ant with its aging step: updateAntAges (src/Colony.cu:353-364), the
 // cleared tour of an invalid ant (src/Colony.cu:507-510) and the blend
 // decision of compute_fittness (inc/Colony.cuh:21-30).
-template <bool AGING, int TW, int G>
+template <bool AGING, int TW, int G, class ROWS>
 __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
-                                     const int16_t *sids, const float *scw, const float *smean,
-                                     int lane) {
+                                     const ROWS &rows, int lane) {
   AntCtx a;
   a.blend = false;
   a.ratio = 0.0f;
@@ -678,9 +721,9 @@ __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, f
     if (a.blend) a.ratio = __fdiv_rn(__int2float_rn(age), __int2float_rn(c.min_ret));
   }
   if (AGING && a.blend)
-    staged_ant_body<TW, G, true>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+    staged_ant_body<TW, G, true, false>(c, k, iter, wbuf, rows, a, lane);
   else
-    staged_ant_body<TW, G, false>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+    staged_ant_body<TW, G, false, false>(c, k, iter, wbuf, rows, a, lane);
 }
 
 template <bool MULTI, bool AGING>
@@ -799,6 +842,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
   float *wbuf = reinterpret_cast<float *>(smem_staged + L.table) + (size_t)warp * 32;
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_staged + L.table + (size_t)warps * 128);
   __shared__ int flag;
+  const TableRows<SP> rows{sids, scw, smean};
 
   const int grid = gridDim.x;
   const int B = AGING ? c.plan[0] : 0;
@@ -859,7 +903,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
         a.blend = true;
         a.ratio = ratio;
         a.meanc = 0.0f;
-        staged_ant_body<TW, G, false, true>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+        staged_ant_body<TW, G, false, true>(c, k, iter, wbuf, rows, a, lane);
       }
       __syncthreads();
     }
@@ -881,7 +925,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
   const int others = c.m - B;
   for (int i = ((int)blockIdx.x - base) + P * warp; i < others; i += P * warps) {
     if (!AGING) {
-      construct_ant_staged<false, TW, G>(c, i, iter, wbuf, sids, scw, smean, lane);
+      construct_ant_staged<false, TW, G>(c, i, iter, wbuf, rows, lane);
       continue;
     }
     const int k = plan_list[B + i];
@@ -894,7 +938,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
     a.blend = false;
     a.ratio = 0.0f;
     a.meanc = 0.0f;
-    staged_ant_body<TW, G, false>(c, k, iter, wbuf, sids, scw, smean, a, lane);
+    staged_ant_body<TW, G, false, false>(c, k, iter, wbuf, rows, a, lane);
   }
 }
 
@@ -908,8 +952,173 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32) k_construct_direct(Colon
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
   const uint32_t iter = c.st->iteration;
   for (int k = blockIdx.x * warps + warp; k < c.m; k += gridDim.x * warps)
-    construct_ant_staged<AGING, TW, G>(c, k, iter, wb + warp * 32, c.nn16, c.choice_nn, c.mean,
-                                       lane);
+    construct_ant_staged<AGING, TW, G>(c, k, iter, wb + warp * 32,
+                                       TableRows<4 * G>{c.nn16, c.choice_nn, c.mean}, lane);
+}
+
+// ---------------------------------------------------------------------------
+// Candidate table split over a thread-block cluster (k <= 32, n <= 8192, a
+// table too large for one CTA): cluster rank r holds rows r*1024 .. r*1024 +
+// 1023 (choice values, int16 ids, aging row means) at the same offsets as
+// every other rank.  Each CTA stages its slice with TMA bulk copies; after a
+// cluster barrier the ants read every row from its owner's shared memory
+// (mapa + ld.shared::cluster) with the staged step loop; a second barrier
+// keeps each slice alive until the whole cluster is done.  Every thread
+// reaches both barriers on every path (a copy that timed out only records
+// the error).  All CTAs share all ants.
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_size() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n\t"
+      "barrier.cluster.wait.acquire.aligned;" ::
+          : "memory");
+}
+
+template <bool AGING, int TW, int G>
+__global__ void __launch_bounds__(kStagedMaxWarps * 32) k_construct_cluster(ColonyDev c) {
+  extern __shared__ __align__(128) unsigned char smem_cl[];
+  constexpr int SP = 4 * G;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+  const StagedLayout L = staged_layout(kClusterRows, kClusterRows, SP, AGING);
+  float *scw = reinterpret_cast<float *>(smem_cl);
+  int16_t *sids = reinterpret_cast<int16_t *>(smem_cl + L.ids_off);
+  float *smean = reinterpret_cast<float *>(smem_cl + L.mean_off);
+  float *wbuf = reinterpret_cast<float *>(smem_cl + L.table) + (size_t)warp * 32;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_cl + L.table + (size_t)warps * 128);
+  __shared__ int flag, all_ok;
+
+  const int r0 = (int)cluster_rank() * kClusterRows;
+  const int rows_here = max(0, min(kClusterRows, c.n - r0));
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // sizes rounded up to 16 bytes (the buffers carry 16 bytes of slack)
+    const uint32_t cw_bytes = (uint32_t)rows_here * SP * 4u;
+    const uint32_t id_bytes = ((uint32_t)rows_here * SP * 2u + 15u) & ~15u;
+    const uint32_t mean_bytes = AGING ? (((uint32_t)rows_here * 4u + 15u) & ~15u) : 0u;
+    const uint32_t total = cw_bytes + id_bytes + mean_bytes;
+    int ok = 1;
+    if (total) {
+      mbar_arrive_expect_tx(bar, total);
+      constexpr uint32_t kPiece = 32768;
+      const char *g = reinterpret_cast<const char *>(c.choice_nn + (size_t)r0 * SP);
+      for (uint32_t o = 0; o < cw_bytes; o += kPiece)
+        tma_load_1d(reinterpret_cast<char *>(scw) + o, g + o, min(kPiece, cw_bytes - o), bar);
+      g = reinterpret_cast<const char *>(c.nn16 + (size_t)r0 * SP);
+      for (uint32_t o = 0; o < id_bytes; o += kPiece)
+        tma_load_1d(reinterpret_cast<char *>(sids) + o, g + o, min(kPiece, id_bytes - o), bar);
+      if (AGING) tma_load_1d(smean, c.mean + r0, mean_bytes, bar);
+      ok = mbar_wait_bounded(bar, 0, c.st) ? 1 : 0;
+    }
+    flag = ok;
+  }
+  __syncthreads();
+  cluster_barrier();  // every slice of the cluster is in place
+  if (threadIdx.x == 0) {
+    // ants read every slice: run them only when every CTA staged its own
+    int all = 1;
+    for (uint32_t r = 0; r < cluster_size(); r++) {
+      uint32_t a;
+      int v;
+      asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(&flag)), "r"(r));
+      asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(a));
+      all &= v;
+    }
+    all_ok = all;
+  }
+  __syncthreads();
+  if (all_ok) {
+    const ClusterRows<SP> rows{smem_u32(sids), smem_u32(scw), smem_u32(smean)};
+    const uint32_t iter = c.st->iteration;
+    for (int k = blockIdx.x * warps + warp; k < c.m; k += gridDim.x * warps)
+      construct_ant_staged<AGING, TW, G>(c, k, iter, wbuf, rows, lane);
+  }
+  __syncthreads();
+  cluster_barrier();  // no slice is released while another CTA may read it
+}
+
+size_t construct_cluster_smem_bytes(int sp, bool aging, int warps) {
+  return staged_layout(kClusterRows, kClusterRows, sp, aging).table + (size_t)warps * 128 + 16;
+}
+
+namespace {
+template <bool AGING, int TW, int G>
+cudaError_t cluster_launch_t(const ColonyDev &c, int grid, int warps, int cs, cudaStream_t s,
+                             int *max_clusters) {
+  const size_t smem = construct_cluster_smem_bytes(4 * G, AGING, warps);
+  if (max_clusters) {
+    // the query, at planning time, opens the kernel to any warp count, so a
+    // launch (possibly under stream capture) sets no attribute
+    const size_t most = construct_cluster_smem_bytes(4 * G, AGING, kStagedMaxWarps);
+    cudaError_t e = cudaFuncSetAttribute(k_construct_cluster<AGING, TW, G>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(warps * 32);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cs;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (max_clusters) return cudaOccupancyMaxActiveClusters(max_clusters, k_construct_cluster<AGING, TW, G>, &cfg);
+  return cudaLaunchKernelEx(&cfg, k_construct_cluster<AGING, TW, G>, c);
+}
+template <bool AGING, int G>
+cudaError_t cluster_launch_tw(const ColonyDev &c, int grid, int warps, int cs, cudaStream_t s,
+                              int *max_clusters) {
+  if (c.n <= 2048) return cluster_launch_t<AGING, 2, G>(c, grid, warps, cs, s, max_clusters);
+  if (c.n <= 4096) return cluster_launch_t<AGING, 4, G>(c, grid, warps, cs, s, max_clusters);
+  return cluster_launch_t<AGING, 8, G>(c, grid, warps, cs, s, max_clusters);
+}
+template <int G>
+cudaError_t cluster_launch_g(const ColonyDev &c, int grid, int warps, int cs, cudaStream_t s,
+                             int *max_clusters) {
+  return c.aging ? cluster_launch_tw<true, G>(c, grid, warps, cs, s, max_clusters)
+                 : cluster_launch_tw<false, G>(c, grid, warps, cs, s, max_clusters);
+}
+cudaError_t cluster_dispatch(const ColonyDev &c, int grid, int warps, int cs, cudaStream_t s,
+                             int *max_clusters) {
+  if (c.n > kDirectMaxCities || c.K > 32 || c.ldk != staged_pitch(c.K) || !c.nn16 ||
+      warps < 1 || warps > kStagedMaxWarps || cs < 1 || cs > 8 ||
+      cs * kClusterRows < c.n || (max_clusters == nullptr && grid % cs))
+    return cudaErrorInvalidValue;
+  switch (c.ldk) {
+    case 16: return cluster_launch_g<4>(c, grid, warps, cs, s, max_clusters);
+    case 20: return cluster_launch_g<5>(c, grid, warps, cs, s, max_clusters);
+    case 24: return cluster_launch_g<6>(c, grid, warps, cs, s, max_clusters);
+    default: return cluster_launch_g<8>(c, grid, warps, cs, s, max_clusters);
+  }
+}
+}  // namespace
+
+cudaError_t query_construct_cluster(const ColonyDev &c, int warps, int cs, int *max_clusters) {
+  *max_clusters = 0;
+  return cluster_dispatch(c, cs, warps, cs, nullptr, max_clusters);
+}
+
+cudaError_t launch_construct_cluster(const ColonyDev &c, int grid, int warps, int cs,
+                                     cudaStream_t s) {
+  return cluster_dispatch(c, grid, warps, cs, s, nullptr);
 }
 
 namespace {
@@ -1121,17 +1330,17 @@ __global__ void __launch_bounds__(512) k_batch_construct(const ColonyDev *__rest
       if (!s_ok) break;
       if (warp < w.z) {
         if (n <= 1024)
-          construct_ant_staged<AGING, 1, G>(c, w.y + warp, c.st->iteration, swbuf, sids, scw,
-                                            smean, lane);
+          construct_ant_staged<AGING, 1, G>(c, w.y + warp, c.st->iteration, swbuf,
+                                            TableRows<4 * G>{sids, scw, smean}, lane);
         else
-          construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf, sids, scw,
-                                            smean, lane);
+          construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf,
+                                            TableRows<4 * G>{sids, scw, smean}, lane);
       }
     } else if (!MULTI && c.nn16 && c.ldk == 4 * G && c.n <= 2048) {
       // Too large to stage: the same step loop on rows read from L2.
       if (warp < w.z)
-        construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf, c.nn16,
-                                          c.choice_nn, c.mean, lane);
+        construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf,
+                                          TableRows<4 * G>{c.nn16, c.choice_nn, c.mean}, lane);
     } else if (warp < w.z) {
       construct_ant<MULTI, AGING, false>(c, w.y + warp, c.st->iteration, tabu, cend, wbuf,
                                          nullptr, nullptr, nullptr, (c.K + 31) >> 5, lane);

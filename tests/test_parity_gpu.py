@@ -156,17 +156,33 @@ def test_staged_blend_ants_match_oracle(m, six, iters):
     run_pair(p, d, iters, ctx=f"blend m{m}")
 
 
-@pytest.mark.parametrize("n,k,aging", [(1500, 32, 0), (3000, 20, 1), (5000, 32, 0)])
-def test_direct_kernel_matches_oracle(n, k, aging):
-    """k <= 32 with a candidate table too large for shared memory: the step
-    loop on rows read from L2, with the tabu list in 2, 4 and 8 registers per
-    lane, reproduces the oracle (aging: through the blend and its fallback)."""
+@pytest.mark.parametrize("mode", ["direct", "cluster"])
+@pytest.mark.parametrize("n,k,aging", [(1500, 32, 0), (3000, 20, 1), (5000, 32, 0),
+                                       (8192, 16, 0)])
+def test_large_table_kernels_match_oracle(n, k, aging, mode):
+    """k <= 32 with a candidate table too large for one CTA's shared memory:
+    the step loop on rows read from L2 (direct) or on the table split over a
+    cluster of ceil(n/1024) CTAs read through distributed shared memory
+    (cluster: 2, 3, 5 and 8 CTAs), with the tabu list in 2, 4, 8 and 8
+    registers per lane, reproduces the oracle (aging: through the blend and
+    its fallback)."""
     _, _, d = instance(n, 50 + n, kind="clustered")
-    p = params(num_ants=24, beta=2.0, rho=0.2, cand_k=k, seed=n, aging=aging, **FAST_MODE)
+    cm = _abi.ACO_CONSTRUCT_DIRECT if mode == "direct" else _abi.ACO_CONSTRUCT_CLUSTER
+    p = params(num_ants=24, beta=2.0, rho=0.2, cand_k=k, seed=n, aging=aging,
+               construct_mode=cm, **FAST_MODE)
     if aging:
         (p.min_retirement_age, p.max_retirement_age, p.global_performance,
          p.min_population_limit) = (3, 6, 2, 20)
-    run_pair(p, d, 10 if aging else 3, ctx=f"direct n{n}")
+    run_pair(p, d, 10 if aging else 3, ctx=f"{mode} n{n}")
+
+
+def test_cluster_kernel_many_ants_matches_oracle():
+    """The cluster kernel with several ant warps per CTA and more ants than
+    one pass of the grid holds (n=2100: clusters of 3)."""
+    _, _, d = instance(2100, 91, kind="clustered")
+    p = params(num_ants=700, beta=2.0, rho=0.1, cand_k=24, seed=91,
+               construct_mode=_abi.ACO_CONSTRUCT_CLUSTER, **FAST_MODE)
+    run_pair(p, d, 2, ctx="cluster m700")
 
 
 @pytest.mark.parametrize("apb", [1, 2, 8, 16])
