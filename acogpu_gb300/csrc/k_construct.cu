@@ -546,7 +546,14 @@ struct ClusterRows {
 //    prefixes never decrease, so the crossing lanes form a suffix of the warp
 //    and the first of them is a ballot + ffs; the crossing candidate always
 //    has a non-zero weight.  No crossing (S = 0, or u*S rounding up to S)
-//    takes the fallback, as the reference does.
+//    takes the fallback, as the reference does.  An infinite weight (two
+//    cities at distance 0) turns the masked product inf*0 into a NaN prefix
+//    in the lanes before it, where the reference has a finite one, so the
+//    test is written acc > rnd || rnd is NaN: the same as !(s <= rnd) for
+//    every prefix the reference forms (its prefixes are NaN only when a
+//    weight is, and then S and rnd are NaN too), false for the masks' NaNs.
+//    With S = +inf this gives the reference's walk: past the row into the
+//    fallback for rnd = +inf, candidate 0 for rnd = NaN (u = 0).
 // The next row is loaded before the (rare) fallback test resolves.  The
 // uniforms of 32 consecutive steps are computed one per lane and broadcast;
 // the tour positions of the current 32-step block stay in one register per
@@ -606,7 +613,8 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
         sum = __fadd_rn(sum, p.w);
       }
       const float rnd = __fmul_rn(u, sum);
-      const unsigned hit = __ballot_sync(kFull, !(acc <= rnd));
+      // The reference's !(s <= rnd), with the mask's NaNs (inf*0) left out.
+      const unsigned hit = __ballot_sync(kFull, acc > rnd || rnd != rnd);
       int next = __shfl_sync(kFull, id, (__ffs(hit) - 1) & 31);
       // The next row, loaded before the fallback test resolves (an in-range
       // stand-in keeps the loads inside the table) and reloaded if the

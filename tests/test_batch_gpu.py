@@ -109,3 +109,36 @@ def test_uneven_batch_properties():
     assert b.tours_built() - built == 2 * sum(min(n, 1024) for n in sizes)
     assert np.all(b.glob_best() <= after)
     b.close()
+
+
+def test_coincident_cities_batch_matches_general_kernel():
+    """Instances with coincident triples (infinite candidate weights at
+    positions 0 and 1, +inf weight sums) in one batch: the staged and L2-row
+    items reproduce single colonies on the general kernel, whose ordered fold
+    needs no masked products."""
+    insts = []
+    for i, n in enumerate([300, 1500, 90]):
+        x, y = instances.uniform_instance(n, seed=40 + i)
+        x, y = np.array(x), np.array(y)
+        pick = np.random.default_rng(40 + i).choice(n, 3 * (n // 30), replace=False)
+        for a, b2, c2 in pick.reshape(-1, 3):
+            x[b2] = x[c2] = x[a]
+            y[b2] = y[c2] = y[a]
+        insts.append((x, y))
+    p = fast_params()
+    cap = 64
+    b = aco.Batch(insts, params=p, num_ants=cap)
+    b.initialize()
+    b.run(4)
+    b.synchronize()
+    g = _abi.AcoParams.from_buffer_copy(p)
+    g.construct_mode = _abi.ACO_CONSTRUCT_GLOBAL
+    for i, inst in enumerate(insts):
+        c = single(inst, g, i, cap)
+        for _ in range(4):
+            c.constructSolution()
+        v = b.colony(i)
+        assert np.array_equal(v.tours(), c.tours()), f"instance {i}: tours"
+        assert np.array_equal(v.pheromone().view(np.uint32), c.pheromone().view(np.uint32)), i
+        c.close()
+    b.close()

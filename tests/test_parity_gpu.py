@@ -176,6 +176,33 @@ def test_large_table_kernels_match_oracle(n, k, aging, mode):
     run_pair(p, d, 10 if aging else 3, ctx=f"{mode} n{n}")
 
 
+def coincident_instance(n, seed, groups):
+    """Uniform cities with `groups` triples of them moved onto one point:
+    distance 0, infinite heuristic weights at candidate positions 0 and 1 of
+    their rows, and sums of candidate weights that are +inf."""
+    from acogpu_gb300 import instances
+    x, y = instances.uniform_instance(n, box=10000, seed=seed)
+    x, y = np.array(x), np.array(y)
+    pick = np.random.default_rng(seed).choice(n, 3 * groups, replace=False).reshape(groups, 3)
+    for a, b, c in pick:
+        x[b] = x[c] = x[a]
+        y[b] = y[c] = y[a]
+    return instances.euc2d_distances(x, y)
+
+
+@pytest.mark.parametrize("mode", [_abi.ACO_CONSTRUCT_GLOBAL, _abi.ACO_CONSTRUCT_STAGED,
+                                  _abi.ACO_CONSTRUCT_DIRECT, _abi.ACO_CONSTRUCT_CLUSTER])
+def test_coincident_cities_match_oracle(mode):
+    """Infinite candidate weights anywhere in a row (not only first): the
+    reference's walk then ends at candidate 0 (u*S NaN) or in the fallback,
+    and every construction kernel takes the same branch."""
+    d = coincident_instance(1100, 31, 40)
+    assert (d[~np.eye(1100, dtype=bool)] == 0).any()
+    p = params(num_ants=96, beta=2.0, rho=0.2, cand_k=20, seed=31, construct_mode=mode,
+               **FAST_MODE)
+    run_pair(p, d, 3, ctx=f"coincident mode{mode}")
+
+
 def test_cluster_kernel_many_ants_matches_oracle():
     """The cluster kernel with several ant warps per CTA and more ants than
     one pass of the grid holds (n=2100: clusters of 3)."""
