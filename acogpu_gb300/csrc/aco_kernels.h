@@ -39,6 +39,8 @@ cudaError_t launch_construct(const ColonyDev &c, int ants_per_block, cudaStream_
 // Candidate table staged in shared memory (k <= 32, n <= 2048); at most
 // kStagedMaxWarps warps (ants in flight) per CTA.
 constexpr int kStagedMaxWarps = 16;
+// Launches of at most this many warps per CTA may hold 255 registers a thread.
+constexpr int kWideFallbackWarps = 8;
 // Pitch of the candidate rows (nn, eta_nn, tau_nn, choice_nn, nn16) for
 // k <= 32: the staged step folds pitch/4 groups of four weights, and the
 // pitch takes one of four values so the fold length is a template constant.

@@ -368,13 +368,14 @@ __device__ __forceinline__ uint32_t tw_pick(const uint32_t (&tw)[TW], int t) {
 }
 
 // Largest choice value among unvisited cities (register tabu version).  The
-// plain rule issues the row loads four 128-city chunks at a time, so a scan
-// of n cities waits for ceil(n / 512) L2 round trips, not one per chunk.
-// Inlined: the tabu words must stay in registers (a call would take the
-// array's address and move it to local memory).
+// plain rule issues the row loads FB 128-city chunks at a time, so a scan of
+// n cities waits for ceil(n / (128 FB)) L2 round trips, not one per chunk
+// (FB = 16 holds 64 registers of loads: kernels launched for at most
+// kWideFallbackWarps warps).  Inlined: the tabu words must stay in registers
+// (a call would take the array's address and move it to local memory).
 // WIDE: the blend scan also issues its loads two chunks at a time (more
 // registers; used where the kernel has them to spare).
-template <int TW, bool WIDE>
+template <int TW, bool WIDE, int FB = 4>
 __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
                                                  const uint32_t (&tw)[TW], const AntCtx &a,
                                                  int lane) {
@@ -384,31 +385,45 @@ __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
   const float *trow = c.tau + (size_t)cur * c.ld;
   const float *erow = c.eta + (size_t)cur * c.ld;
   if (!a.blend) {
+    // Four independent running maxima, one per float4 component (each sees
+    // its cities in increasing order, so a strict > keeps the lowest index
+    // of a tie), merged below; visited and out-of-range cities enter as -1,
+    // below every weight, so the scan has no branch.
+    float cw[4] = {-1.0f, -1.0f, -1.0f, -1.0f};
+    int cj[4] = {-1, -1, -1, -1};
 #pragma unroll
-    for (int t0 = 0; t0 < 8 * TW; t0 += 4) {  // n <= 1024 * TW
+    for (int t0 = 0; t0 < 8 * TW; t0 += FB) {  // n <= 1024 * TW
       if (t0 * 128 >= c.n) continue;  // (not break: the loop stays fully unrolled)
-      float4 q[4];
+      float4 q[FB];
 #pragma unroll
-      for (int t = 0; t < 4; t++) {
+      for (int t = 0; t < FB; t++) {
         const int j4 = (t0 + t) * 128 + lane * 4;  // j4 < n implies j4 + 3 < ld (ld % 32 == 0)
         q[t] = j4 < c.n ? __ldcg(reinterpret_cast<const float4 *>(crow + j4))
                         : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
-      for (int t = 0; t < 4; t++) {
+      for (int t = 0; t < FB; t++) {
         const int j4 = (t0 + t) * 128 + lane * 4;
         const uint32_t v =
             __shfl_sync(kFull, tw_pick(tw, (t0 + t) >> 3), ((t0 + t) * 4 + (lane >> 3)) & 31);
-        const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
+        const int left = c.n - j4;  // cities of this float4 inside the instance
+        const uint32_t in = left >= 4 ? 0xfu : (left > 0 ? (1u << left) - 1u : 0u);
+        const uint32_t open = ~(v >> (j4 & 31)) & in;
         const float qq[4] = {q[t].x, q[t].y, q[t].z, q[t].w};
 #pragma unroll
         for (int r = 0; r < 4; r++) {
-          if (!((bits >> r) & 1u) && j4 + r < c.n && qq[r] > bw) {
-            bw = qq[r];
-            bj = j4 + r;
-          }
+          const float x = (open >> r) & 1u ? qq[r] : -1.0f;
+          const bool up = x > cw[r];
+          cw[r] = up ? x : cw[r];
+          cj[r] = up ? j4 + r : cj[r];
         }
       }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const bool take = cj[r] >= 0 && (bj < 0 || cw[r] > bw || (cw[r] == bw && cj[r] < bj));
+      bw = take ? cw[r] : bw;
+      bj = take ? cj[r] : bj;
     }
   } else if (WIDE) {  // aging blend (young ants after convergence): tau and
                       // eta rows, two 128-city chunks at a time
@@ -558,7 +573,7 @@ struct ClusterRows {
 // uniforms of 32 consecutive steps are computed one per lane and broadcast;
 // the tour positions of the current 32-step block stay in one register per
 // lane and are stored together.
-template <int TW, bool BLEND, int G, bool WIDE, class ROWS>
+template <int TW, bool BLEND, int G, bool WIDE, class ROWS, int FB = 4>
 __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t akey, int start,
                                             uint32_t (&tw)[TW], float *wbuf, const ROWS &rows,
                                             AntCtx a, int lane, int64_t &fallbacks) {
@@ -627,7 +642,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
           ok = false;
         } else if (c.fallback == ACO_FALLBACK_BEST) {
           if (!BLEND && a.blend) a.meanc = rows.row_mean(cur);  // pre-blended table
-          next = fallback_best_reg<TW, WIDE>(c, cur, tw, a, lane);
+          next = fallback_best_reg<TW, WIDE, FB>(c, cur, tw, a, lane);
         } else {  // select_local_best on a full row of at most 32 cities (k == n)
           const unsigned um = __ballot_sync(kFull, id >= 0 && !vis);
           next = um ? __shfl_sync(kFull, id, 31 - __clz(um)) : -1;
@@ -656,7 +671,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
 // the step loop (BLEND: the aging fitness blend of every candidate per step;
 // otherwise the weights come blended, or plain, from the table), then the
 // integer length and the transposed successor/predecessor lists.
-template <int TW, int G, bool BLEND, bool WIDE, class ROWS>
+template <int TW, int G, bool BLEND, bool WIDE, class ROWS, int FB = 4>
 __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
                                 const ROWS &rows, AntCtx a, int lane) {
   const int n = c.n;
@@ -675,7 +690,8 @@ __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float 
   reg_mark(tw, start, lane);
 
   int64_t fallbacks = 0;
-  staged_steps<TW, BLEND, G, WIDE>(c, k, akey, start, tw, wbuf, rows, a, lane, fallbacks);
+  staged_steps<TW, BLEND, G, WIDE, ROWS, FB>(c, k, akey, start, tw, wbuf, rows, a, lane,
+                                             fallbacks);
   __syncwarp();
   // Tour length (order-free integer sum) and the transposed successor /
   // predecessor of every city for the row-owned deposit, one edge per lane;
@@ -706,7 +722,7 @@ __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float 
 // One ant with its aging step: updateAntAges (src/Colony.cu:353-364), the
 // cleared tour of an invalid ant (src/Colony.cu:507-510) and the blend
 // decision of compute_fittness (inc/Colony.cuh:21-30).
-template <bool AGING, int TW, int G, class ROWS>
+template <bool AGING, int TW, int G, class ROWS, int FB = 4>
 __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
                                      const ROWS &rows, int lane) {
   AntCtx a;
@@ -729,9 +745,9 @@ __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, f
     if (a.blend) a.ratio = __fdiv_rn(__int2float_rn(age), __int2float_rn(c.min_ret));
   }
   if (AGING && a.blend)
-    staged_ant_body<TW, G, true, false>(c, k, iter, wbuf, rows, a, lane);
+    staged_ant_body<TW, G, true, false, ROWS, FB>(c, k, iter, wbuf, rows, a, lane);
   else
-    staged_ant_body<TW, G, false, false>(c, k, iter, wbuf, rows, a, lane);
+    staged_ant_body<TW, G, false, false, ROWS, FB>(c, k, iter, wbuf, rows, a, lane);
 }
 
 template <bool MULTI, bool AGING>
@@ -993,8 +1009,9 @@ __device__ __forceinline__ void cluster_barrier() {
           : "memory");
 }
 
-template <bool AGING, int TW, int G>
-__global__ void __launch_bounds__(kStagedMaxWarps * 32) k_construct_cluster(ColonyDev c) {
+template <bool AGING, int TW, int G, int FB>
+__global__ void __launch_bounds__((FB > 4 ? kWideFallbackWarps : kStagedMaxWarps) * 32)
+    k_construct_cluster(ColonyDev c) {
   extern __shared__ __align__(128) unsigned char smem_cl[];
   constexpr int SP = 4 * G;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
@@ -1053,7 +1070,7 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32) k_construct_cluster(Colo
     const ClusterRows<SP> rows{smem_u32(sids), smem_u32(scw), smem_u32(smean)};
     const uint32_t iter = c.st->iteration;
     for (int k = blockIdx.x * warps + warp; k < c.m; k += gridDim.x * warps)
-      construct_ant_staged<AGING, TW, G>(c, k, iter, wbuf, rows, lane);
+      construct_ant_staged<AGING, TW, G, ClusterRows<SP>, FB>(c, k, iter, wbuf, rows, lane);
   }
   __syncthreads();
   cluster_barrier();  // no slice is released while another CTA may read it
@@ -1064,7 +1081,7 @@ size_t construct_cluster_smem_bytes(int sp, bool aging, int warps) {
 }
 
 namespace {
-template <bool AGING, int TW, int G>
+template <bool AGING, int TW, int G, int FB>
 cudaError_t cluster_launch_t(const ColonyDev &c, int grid, int warps, int cs, cudaStream_t s,
                              int *max_clusters) {
   const size_t smem = construct_cluster_smem_bytes(4 * G, AGING, warps);
@@ -1072,7 +1089,7 @@ cudaError_t cluster_launch_t(const ColonyDev &c, int grid, int warps, int cs, cu
     // the query, at planning time, opens the kernel to any warp count, so a
     // launch (possibly under stream capture) sets no attribute
     const size_t most = construct_cluster_smem_bytes(4 * G, AGING, kStagedMaxWarps);
-    cudaError_t e = cudaFuncSetAttribute(k_construct_cluster<AGING, TW, G>,
+    cudaError_t e = cudaFuncSetAttribute(k_construct_cluster<AGING, TW, G, FB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
     if (e != cudaSuccess) return e;
   }
@@ -1088,15 +1105,21 @@ cudaError_t cluster_launch_t(const ColonyDev &c, int grid, int warps, int cs, cu
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  if (max_clusters) return cudaOccupancyMaxActiveClusters(max_clusters, k_construct_cluster<AGING, TW, G>, &cfg);
-  return cudaLaunchKernelEx(&cfg, k_construct_cluster<AGING, TW, G>, c);
+  if (max_clusters)
+    return cudaOccupancyMaxActiveClusters(max_clusters, k_construct_cluster<AGING, TW, G, FB>, &cfg);
+  return cudaLaunchKernelEx(&cfg, k_construct_cluster<AGING, TW, G, FB>, c);
 }
 template <bool AGING, int G>
 cudaError_t cluster_launch_tw(const ColonyDev &c, int grid, int warps, int cs, cudaStream_t s,
                               int *max_clusters) {
-  if (c.n <= 2048) return cluster_launch_t<AGING, 2, G>(c, grid, warps, cs, s, max_clusters);
-  if (c.n <= 4096) return cluster_launch_t<AGING, 4, G>(c, grid, warps, cs, s, max_clusters);
-  return cluster_launch_t<AGING, 8, G>(c, grid, warps, cs, s, max_clusters);
+  // n > 2048 with few ants per CTA: the fallback scan with 16 chunks in flight
+  const bool wide = warps <= kWideFallbackWarps;
+  if (c.n <= 2048) return cluster_launch_t<AGING, 2, G, 4>(c, grid, warps, cs, s, max_clusters);
+  if (c.n <= 4096)
+    return wide ? cluster_launch_t<AGING, 4, G, 16>(c, grid, warps, cs, s, max_clusters)
+                : cluster_launch_t<AGING, 4, G, 4>(c, grid, warps, cs, s, max_clusters);
+  return wide ? cluster_launch_t<AGING, 8, G, 16>(c, grid, warps, cs, s, max_clusters)
+              : cluster_launch_t<AGING, 8, G, 4>(c, grid, warps, cs, s, max_clusters);
 }
 template <int G>
 cudaError_t cluster_launch_g(const ColonyDev &c, int grid, int warps, int cs, cudaStream_t s,
@@ -1121,7 +1144,13 @@ cudaError_t cluster_dispatch(const ColonyDev &c, int grid, int warps, int cs, cu
 
 cudaError_t query_construct_cluster(const ColonyDev &c, int warps, int cs, int *max_clusters) {
   *max_clusters = 0;
-  return cluster_dispatch(c, cs, warps, cs, nullptr, max_clusters);
+  // Both fallback widths (the query also opens each kernel's shared memory):
+  // the launch picks one by its final warp count.
+  int wide = 0, narrow = 0;
+  cudaError_t e = cluster_dispatch(c, cs, kWideFallbackWarps, cs, nullptr, &wide);
+  if (e == cudaSuccess) e = cluster_dispatch(c, cs, kStagedMaxWarps, cs, nullptr, &narrow);
+  if (e == cudaSuccess) *max_clusters = warps <= kWideFallbackWarps ? wide : narrow;
+  return e;
 }
 
 cudaError_t launch_construct_cluster(const ColonyDev &c, int grid, int warps, int cs,
