@@ -314,7 +314,7 @@ def run_ours(args, rank, world, local):
                               "pheromone": stage[4] / args.steps},
         "fallback_rate": fallbacks / max(1, tours * (N_CITIES - 1)),
         "gpu_launches": int(launches) * world,
-        "roofline": {"bound": "hbm", "kernel": "k_construct", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "k_construct_staged", "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm else None,
                      "algorithmic_bytes_per_launch": bytes_c / args.steps,
@@ -451,8 +451,12 @@ def run_large(args, rank, world, local):
                                   "epilogue": stage[2] / args.steps,
                                   "pheromone": stage[4] / args.steps},
             "fallback_rate": fallbacks / max(1, tours * 4095), "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": "k_construct", "achieved": achieved,
-                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None},
+            "roofline": {"bound": "hbm", "kernel": "k_construct_cluster", "achieved": achieved,
+                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm else None,
+                         "algorithmic_bytes_per_launch": bytes_c / args.steps,
+                         "traffic": profiled_traffic("construct_cluster_as_n4096.md"),
+                         "traffic_source": "profiles/construct_cluster_as_n4096.md (ncu)"},
             "best": best, "clocks": clk.summary()}
 
 
