@@ -426,13 +426,16 @@ __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
       bj = take ? cj[r] : bj;
     }
   } else if (WIDE) {  // aging blend (young ants after convergence): tau and
-                      // eta rows, two 128-city chunks at a time
+                      // eta rows, four 128-city chunks at a time, the same
+                      // four branch-free running maxima
+    float cw[4] = {-1.0f, -1.0f, -1.0f, -1.0f};
+    int cj[4] = {-1, -1, -1, -1};
 #pragma unroll
-    for (int t0 = 0; t0 < 8 * TW; t0 += 2) {  // n <= 1024 * TW
+    for (int t0 = 0; t0 < 8 * TW; t0 += 4) {  // n <= 1024 * TW
       if (t0 * 128 >= c.n) continue;
-      float4 tq[2], eq[2];
+      float4 tq[4], eq[4];
 #pragma unroll
-      for (int t = 0; t < 2; t++) {
+      for (int t = 0; t < 4; t++) {
         const int j4 = (t0 + t) * 128 + lane * 4;
         const bool in = j4 < c.n;
         tq[t] = in ? __ldcg(reinterpret_cast<const float4 *>(trow + j4))
@@ -441,24 +444,30 @@ __device__ __forceinline__ int fallback_best_reg(const ColonyDev &c, int cur,
                    : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
-      for (int t = 0; t < 2; t++) {
+      for (int t = 0; t < 4; t++) {
         const int j4 = (t0 + t) * 128 + lane * 4;
         const uint32_t v =
             __shfl_sync(kFull, tw_pick(tw, (t0 + t) >> 3), ((t0 + t) * 4 + (lane >> 3)) & 31);
-        const uint32_t bits = (v >> (j4 & 31)) & 0xfu;
+        const int left = c.n - j4;
+        const uint32_t in = left >= 4 ? 0xfu : (left > 0 ? (1u << left) - 1u : 0u);
+        const uint32_t open = ~(v >> (j4 & 31)) & in;
         const float ta[4] = {tq[t].x, tq[t].y, tq[t].z, tq[t].w};
         const float ea[4] = {eq[t].x, eq[t].y, eq[t].z, eq[t].w};
 #pragma unroll
         for (int r = 0; r < 4; r++) {
-          if (!((bits >> r) & 1u) && j4 + r < c.n) {
-            const float q = blend_fitness(ta[r], ea[r], a.meanc, a.ratio, c.use_alpha, c.alpha);
-            if (q > bw) {
-              bw = q;
-              bj = j4 + r;
-            }
-          }
+          const float q = blend_fitness(ta[r], ea[r], a.meanc, a.ratio, c.use_alpha, c.alpha);
+          const float x = (open >> r) & 1u ? q : -1.0f;
+          const bool up = x > cw[r];
+          cw[r] = up ? x : cw[r];
+          cj[r] = up ? j4 + r : cj[r];
         }
       }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const bool take = cj[r] >= 0 && (bj < 0 || cw[r] > bw || (cw[r] == bw && cj[r] < bj));
+      bw = take ? cw[r] : bw;
+      bj = take ? cj[r] : bj;
     }
   } else {  // aging blend, one 128-city chunk per round trip
     for (int base = 0; base < c.n; base += 128) {
@@ -910,16 +919,37 @@ __global__ void __launch_bounds__(kStagedMaxWarps * 32)
       const float4 *tau4 = reinterpret_cast<const float4 *>(c.tau_nn);
       const float4 *eta4 = reinterpret_cast<const float4 *>(c.eta_nn);
       float4 *scw4 = reinterpret_cast<float4 *>(scw);
-      for (int t = threadIdx.x; t < n * G; t += blockDim.x) {
-        const int j = t / G, r0 = (t - j * G) * 4;
-        const float4 tv = tau4[t], ev = __ldg(eta4 + t);
-        const float mj = smean[j];
-        float4 w;
-        w.x = r0 + 0 < c.K ? blend_fitness(tv.x, ev.x, mj, ratio, c.use_alpha, c.alpha) : 0.0f;
-        w.y = r0 + 1 < c.K ? blend_fitness(tv.y, ev.y, mj, ratio, c.use_alpha, c.alpha) : 0.0f;
-        w.z = r0 + 2 < c.K ? blend_fitness(tv.z, ev.z, mj, ratio, c.use_alpha, c.alpha) : 0.0f;
-        w.w = r0 + 3 < c.K ? blend_fitness(tv.w, ev.w, mj, ratio, c.use_alpha, c.alpha) : 0.0f;
-        scw4[t] = w;
+      // Four entries per thread per round: their eight loads are issued
+      // before any is used, so the build waits for ceil(nG / 4T) L2 round
+      // trips instead of ceil(nG / T).
+      constexpr int kBuildBatch = 4;
+      const int stride = blockDim.x;
+      for (int t0 = threadIdx.x; t0 < n * G; t0 += kBuildBatch * stride) {
+        float4 tv[kBuildBatch], ev[kBuildBatch];
+#pragma unroll
+        for (int u = 0; u < kBuildBatch; u++) {
+          const int t = t0 + u * stride;
+          const bool in = t < n * G;
+          tv[u] = in ? tau4[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+          ev[u] = in ? __ldg(eta4 + t) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < kBuildBatch; u++) {
+          const int t = t0 + u * stride;
+          if (t >= n * G) break;
+          const int j = t / G, r0 = (t - j * G) * 4;
+          const float mj = smean[j];
+          float4 w;
+          w.x = r0 + 0 < c.K ? blend_fitness(tv[u].x, ev[u].x, mj, ratio, c.use_alpha, c.alpha)
+                             : 0.0f;
+          w.y = r0 + 1 < c.K ? blend_fitness(tv[u].y, ev[u].y, mj, ratio, c.use_alpha, c.alpha)
+                             : 0.0f;
+          w.z = r0 + 2 < c.K ? blend_fitness(tv[u].z, ev[u].z, mj, ratio, c.use_alpha, c.alpha)
+                             : 0.0f;
+          w.w = r0 + 3 < c.K ? blend_fitness(tv[u].w, ev[u].w, mj, ratio, c.use_alpha, c.alpha)
+                             : 0.0f;
+          scw4[t] = w;
+        }
       }
       __syncthreads();
       if (warp == 0) {
