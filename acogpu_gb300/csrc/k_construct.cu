@@ -582,7 +582,7 @@ struct ClusterRows {
 // uniforms of 32 consecutive steps are computed one per lane and broadcast;
 // the tour positions of the current 32-step block stay in one register per
 // lane and are stored together.
-template <int TW, bool BLEND, int G, bool WIDE, class ROWS, int FB = 4>
+template <int TW, bool BLEND, int G, bool WIDE, class ROWS, int FB = 4, bool LEAN = false>
 __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t akey, int start,
                                             uint32_t (&tw)[TW], float *wbuf, const ROWS &rows,
                                             AntCtx a, int lane, int64_t &fallbacks) {
@@ -622,20 +622,24 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
       wbuf[lane] = w;
       __syncwarp();
       // Two independent chains: this lane's prefix and the full sum S (the
-      // second fills the first's latency gaps and saves a broadcast).
+      // second fills the first's latency gaps and saves a broadcast).  LEAN
+      // (launches with many warps a scheduler, bound by issue rather than by
+      // one ant's latency): S is lane 31's prefix -- the same adds in the
+      // same order -- broadcast, for 4G fewer instructions a step.
       float acc = 0.0f, sum = 0.0f;
 #pragma unroll
       for (int g = 0; g < G; g++) {
         const float4 p = wbuf4[g];
         acc = __fmaf_rn(p.x, incl[4 * g + 0], acc);
-        sum = __fadd_rn(sum, p.x);
+        if constexpr (!LEAN) sum = __fadd_rn(sum, p.x);
         acc = __fmaf_rn(p.y, incl[4 * g + 1], acc);
-        sum = __fadd_rn(sum, p.y);
+        if constexpr (!LEAN) sum = __fadd_rn(sum, p.y);
         acc = __fmaf_rn(p.z, incl[4 * g + 2], acc);
-        sum = __fadd_rn(sum, p.z);
+        if constexpr (!LEAN) sum = __fadd_rn(sum, p.z);
         acc = __fmaf_rn(p.w, incl[4 * g + 3], acc);
-        sum = __fadd_rn(sum, p.w);
+        if constexpr (!LEAN) sum = __fadd_rn(sum, p.w);
       }
+      if constexpr (LEAN) sum = __shfl_sync(kFull, acc, 31);
       const float rnd = __fmul_rn(u, sum);
       // The reference's !(s <= rnd), with the mask's NaNs (inf*0) left out.
       const unsigned hit = __ballot_sync(kFull, acc > rnd || rnd != rnd);
@@ -680,7 +684,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
 // the step loop (BLEND: the aging fitness blend of every candidate per step;
 // otherwise the weights come blended, or plain, from the table), then the
 // integer length and the transposed successor/predecessor lists.
-template <int TW, int G, bool BLEND, bool WIDE, class ROWS, int FB = 4>
+template <int TW, int G, bool BLEND, bool WIDE, class ROWS, int FB = 4, bool LEAN = false>
 __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
                                 const ROWS &rows, AntCtx a, int lane) {
   const int n = c.n;
@@ -699,7 +703,7 @@ __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float 
   reg_mark(tw, start, lane);
 
   int64_t fallbacks = 0;
-  staged_steps<TW, BLEND, G, WIDE, ROWS, FB>(c, k, akey, start, tw, wbuf, rows, a, lane,
+  staged_steps<TW, BLEND, G, WIDE, ROWS, FB, LEAN>(c, k, akey, start, tw, wbuf, rows, a, lane,
                                              fallbacks);
   __syncwarp();
   // Tour length (order-free integer sum) and the transposed successor /
@@ -731,7 +735,7 @@ __device__ void staged_ant_body(const ColonyDev &c, int k, uint32_t iter, float 
 // One ant with its aging step: updateAntAges (src/Colony.cu:353-364), the
 // cleared tour of an invalid ant (src/Colony.cu:507-510) and the blend
 // decision of compute_fittness (inc/Colony.cuh:21-30).
-template <bool AGING, int TW, int G, class ROWS, int FB = 4>
+template <bool AGING, int TW, int G, class ROWS, int FB = 4, bool LEAN = false>
 __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, float *wbuf,
                                      const ROWS &rows, int lane) {
   AntCtx a;
@@ -754,9 +758,9 @@ __device__ void construct_ant_staged(const ColonyDev &c, int k, uint32_t iter, f
     if (a.blend) a.ratio = __fdiv_rn(__int2float_rn(age), __int2float_rn(c.min_ret));
   }
   if (AGING && a.blend)
-    staged_ant_body<TW, G, true, false, ROWS, FB>(c, k, iter, wbuf, rows, a, lane);
+    staged_ant_body<TW, G, true, false, ROWS, FB, LEAN>(c, k, iter, wbuf, rows, a, lane);
   else
-    staged_ant_body<TW, G, false, false, ROWS, FB>(c, k, iter, wbuf, rows, a, lane);
+    staged_ant_body<TW, G, false, false, ROWS, FB, LEAN>(c, k, iter, wbuf, rows, a, lane);
 }
 
 template <bool MULTI, bool AGING>
@@ -1397,17 +1401,18 @@ __global__ void __launch_bounds__(512) k_batch_construct(const ColonyDev *__rest
       if (!s_ok) break;
       if (warp < w.z) {
         if (n <= 1024)
-          construct_ant_staged<AGING, 1, G>(c, w.y + warp, c.st->iteration, swbuf,
-                                            TableRows<4 * G>{sids, scw, smean}, lane);
+          construct_ant_staged<AGING, 1, G, TableRows<4 * G>, 4, true>(
+              c, w.y + warp, c.st->iteration, swbuf, TableRows<4 * G>{sids, scw, smean}, lane);
         else
-          construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf,
-                                            TableRows<4 * G>{sids, scw, smean}, lane);
+          construct_ant_staged<AGING, 2, G, TableRows<4 * G>, 4, true>(
+              c, w.y + warp, c.st->iteration, swbuf, TableRows<4 * G>{sids, scw, smean}, lane);
       }
     } else if (!MULTI && c.nn16 && c.ldk == 4 * G && c.n <= 2048) {
       // Too large to stage: the same step loop on rows read from L2.
       if (warp < w.z)
-        construct_ant_staged<AGING, 2, G>(c, w.y + warp, c.st->iteration, swbuf,
-                                          TableRows<4 * G>{c.nn16, c.choice_nn, c.mean}, lane);
+        construct_ant_staged<AGING, 2, G, TableRows<4 * G>, 4, true>(
+            c, w.y + warp, c.st->iteration, swbuf,
+            TableRows<4 * G>{c.nn16, c.choice_nn, c.mean}, lane);
     } else if (warp < w.z) {
       construct_ant<MULTI, AGING, false>(c, w.y + warp, c.st->iteration, tabu, cend, wbuf,
                                          nullptr, nullptr, nullptr, (c.K + 31) >> 5, lane);
