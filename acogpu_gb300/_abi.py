@@ -27,6 +27,7 @@ ACO_DEPOSIT_DETERMINISTIC, ACO_DEPOSIT_ATOMIC = 0, 1
 ACO_TAU0_REFERENCE, ACO_TAU0_DORIGO, ACO_TAU0_VALUE = 0, 1, 2
 ACO_CONSTRUCT_AUTO, ACO_CONSTRUCT_GLOBAL, ACO_CONSTRUCT_STAGED = 0, 1, 2
 ACO_CONSTRUCT_DIRECT, ACO_CONSTRUCT_CLUSTER = 3, 4
+ACO_FALLBACK_TIER_AUTO, ACO_FALLBACK_TIER_ON, ACO_FALLBACK_TIER_OFF = 0, 1, 2
 ACO_GEMM_MMA_SYNC, ACO_GEMM_TCGEN05 = 0, 1
 
 TIMER_NAMES = ("init_tour", "tour", "compute_ant_distance", "evaporate_pheromone",
@@ -60,7 +61,8 @@ class AcoParams(ctypes.Structure):
         ("seed", ctypes.c_uint64),
         ("ants_per_block", ctypes.c_int32),
         ("construct_mode", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("fallback_tier", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
     ]
 
 

@@ -77,6 +77,14 @@ struct ColonyDev {
   int32_t *dep_col;
   float *dep_delta;
   int32_t *plan;  // aging, staged: {B, V, blend[B], valid others[V], invalid} (m + 2)
+  // Second tier of the fallback (k <= 32): the t2 nearest neighbours after
+  // the k candidates (row pitch kTier2, -1 padded), their choice values and
+  // the largest choice value of the row outside candidates and tier, both
+  // rewritten by the row pass every iteration; t2 = 0 without a tier.
+  const int32_t *nn2;
+  float *t2v;
+  float *mout;
+  int t2;
   ColonyState *st;
   float rho, alpha;
   int use_alpha;
@@ -86,6 +94,8 @@ struct ColonyDev {
 };
 
 __host__ __device__ inline int round_up(int x, int a) { return (x + a - 1) / a * a; }
+
+constexpr int kTier2 = 128;  // row pitch (and most entries) of the fallback's second tier
 
 // (float)1e-18: MIN_PHEROMONE of the reference (inc/default.h:16) as a float.
 __host__ __device__ inline float min_pheromone() { return (float)0.000000000000000001; }

@@ -19,8 +19,10 @@ cudaError_t launch_heuristic_device(const int32_t *dist, int n, int ld, float be
 cudaError_t launch_heuristic_table(const int32_t *dist, int n, int ld, const float *table,
                                    int32_t table_len, float *eta, ColonyState *st, cudaStream_t s);
 // Stable (distance, city) sort of each row, first K entries kept.
+// nn2 (optional, pitch kTier2): neighbours K .. K + t2 - 1 of every row.
 cudaError_t launch_nn_sort_stable(const int32_t *dist, int n, int ld, int K, int ldk, int32_t *nn,
-                                  ColonyState *st, cudaStream_t s);
+                                  ColonyState *st, cudaStream_t s, int32_t *nn2 = nullptr,
+                                  int t2 = 0);
 // The reference CPU quicksort permutation (full rows only).
 cudaError_t launch_nn_ref_qsort(const int32_t *dist, int n, int ld, int32_t *scratch, int32_t *nn,
                                 int ldk, ColonyState *st, cudaStream_t s);

@@ -64,6 +64,7 @@ ColonyDev make_dev(const aco_colony *c) {
   d.succT = c->succT; d.predT = c->predT; d.gbtour = c->gbtour;
   d.age = c->age; d.perf = c->perf; d.valid = c->valid; d.mean = c->mean;
   d.dep_col = c->dep_col; d.dep_delta = c->dep_delta; d.plan = c->plan; d.st = c->st;
+  d.nn2 = c->nn2; d.t2v = c->t2v; d.mout = c->mout; d.t2 = c->t2;
   d.rho = c->p.rho; d.alpha = c->p.alpha; d.use_alpha = c->p.use_alpha;
   d.aging = c->p.aging; d.min_ret = c->p.min_retirement_age;
   d.max_ret = c->p.max_retirement_age; d.global_perf = c->p.global_performance;
@@ -102,6 +103,8 @@ int check_params(const aco_params *p, int n) {
   if (p->ants_per_block < 0 || p->ants_per_block > 16) return ACO_ERR_INVALID_ARGUMENT;
   if (p->construct_mode < ACO_CONSTRUCT_AUTO || p->construct_mode > ACO_CONSTRUCT_CLUSTER)
     return ACO_ERR_INVALID_ARGUMENT;
+  if (p->fallback_tier < ACO_FALLBACK_TIER_AUTO || p->fallback_tier > ACO_FALLBACK_TIER_OFF)
+    return ACO_ERR_INVALID_ARGUMENT;
   if (p->construct_mode == ACO_CONSTRUCT_STAGED && (K > 32 || n > 2048))
     return ACO_ERR_UNSUPPORTED;
   if ((p->construct_mode == ACO_CONSTRUCT_DIRECT || p->construct_mode == ACO_CONSTRUCT_CLUSTER) &&
@@ -133,6 +136,17 @@ int allocate(aco_colony *c) {
   if ((s = dalloc(c, &c->mean, ld))) return s;
   // 16 bytes of slack: the cluster kernel stages slices in 16-byte units
   if (c->K <= 32 && c->n < 32768 && (s = dalloc(c, &c->nn16, n * ldk + 8))) return s;
+  // The fallback's second tier, for the k <= 32 step loop.
+  const bool tier = c->p.fallback_tier == ACO_FALLBACK_TIER_ON ||
+                    (c->p.fallback_tier == ACO_FALLBACK_TIER_AUTO &&
+                     c->p.variant == ACO_ANT_SYSTEM);
+  c->t2 = (tier && c->K <= 32 && c->n < 32768) ? std::min(kTier2, c->n - 1 - c->K) : 0;
+  if (c->t2 < 0) c->t2 = 0;
+  if (c->t2 > 0) {
+    if ((s = dalloc(c, &c->nn2, n * kTier2))) return s;
+    if ((s = dalloc(c, &c->t2v, n * kTier2))) return s;
+    if ((s = dalloc(c, &c->mout, n))) return s;
+  }
   if ((s = dalloc(c, &c->plan, m + 2))) return s;
   if ((s = dalloc(c, &c->dep_col, m + 1))) return s;
   if ((s = dalloc(c, &c->dep_delta, m + 1))) return s;
@@ -455,7 +469,8 @@ int aco_colony_initialize(aco_colony *c) {
 
   // nn-list (Colony::computeNNlist, src/Colony.cu:276-311)
   if (c->p.nn_order == ACO_NN_STABLE) {
-    ACO_CUDA(c, launch_nn_sort_stable(c->dist, n, c->ld, c->K, c->ldk, c->nn, c->st, c->stream),
+    ACO_CUDA(c, launch_nn_sort_stable(c->dist, n, c->ld, c->K, c->ldk, c->nn, c->st, c->stream,
+                                      c->nn2, c->t2),
              "nn sort");
   } else {
     int32_t *scratch = nullptr, *full = nullptr;
@@ -473,6 +488,14 @@ int aco_colony_initialize(aco_colony *c) {
       ACO_CUDA(c, cudaMemcpy2DAsync(c->nn, (size_t)c->ldk * 4, full, (size_t)c->ld * 4,
                                     (size_t)c->K * 4, n, cudaMemcpyDeviceToDevice, c->stream),
                "copy nn");
+      if (c->t2 > 0) {  // the fallback's second tier: neighbours K .. K + t2 - 1
+        ACO_CUDA(c, cudaMemsetAsync(c->nn2, 0xff, (size_t)n * kTier2 * 4, c->stream),
+                 "memset nn2");
+        ACO_CUDA(c, cudaMemcpy2DAsync(c->nn2, (size_t)kTier2 * 4, full + c->K,
+                                      (size_t)c->ld * 4, (size_t)c->t2 * 4, n,
+                                      cudaMemcpyDeviceToDevice, c->stream),
+                 "copy nn2");
+      }
       ACO_CUDA(c, cudaFreeAsync(full, c->stream), "free");
     }
     ACO_CUDA(c, cudaFreeAsync(scratch, c->stream), "free");

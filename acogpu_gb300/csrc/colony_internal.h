@@ -36,6 +36,10 @@ struct aco_colony {
   bool staged = false;      // construction by the staged kernel
   bool direct = false;      // construction by the direct (L2-row) kernel
   int cluster = 0;          // construction by the cluster kernel: CTAs per cluster
+  int32_t *nn2 = nullptr;   // fallback second tier (see ColonyDev)
+  float *t2v = nullptr;
+  float *mout = nullptr;
+  int t2 = 0;
   int staged_grid = 0, staged_warps = 0;
   int num_sms = 0, max_smem_optin = 0;
   std::vector<void *> allocations;

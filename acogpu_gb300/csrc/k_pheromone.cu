@@ -17,7 +17,11 @@
 // fitness, inc/Colony.cuh:29-30; the reference's dev_compute_selection,
 // inc/Colony.cuh:91-99), choice and tau in candidate order, and for aging the
 // row mean of Colony::computePheromoneMean (src/Colony.cu:435-441), a
-// sequential float sum.
+// sequential float sum.  With a fallback second tier (k <= 32) it also writes
+// the choice values of the tier's cities and the largest choice value of the
+// row outside the row itself, its candidates and its tier (marked in a
+// shared bitmap before the row lands; NaNs ignored, as the fallback never
+// picks one).
 //
 // Atomic mode: a float4 evaporation pass, then one red.global.add.f32 per
 // directed edge, then the same row pass without evaporation or deposit.
@@ -51,6 +55,8 @@ __device__ __forceinline__ void pheromone_row_body(const ColonyDev &c, const int
   float *dl = seg_d + (DEPOSIT ? 2 * kDepSeg : 0);
   uint64_t *bar = reinterpret_cast<uint64_t *>(dl + 32);
   int *flag = reinterpret_cast<int *>(bar + 1);
+  uint32_t *nbm = reinterpret_cast<uint32_t *>(flag + 1);  // [ld / 32]: candidates + tier
+  const bool tier = c.t2 > 0;
 
   if (tid == 0) {
     mbar_init(bar, 1);
@@ -58,14 +64,24 @@ __device__ __forceinline__ void pheromone_row_body(const ColonyDev &c, const int
   }
   if (DEPOSIT)
     for (int h = tid; h < ld; h += nthreads) mt[h] = 0;
+  if (tier)
+    for (int w = tid; w < ld / 32; w += nthreads) nbm[w] = 0u;
   __syncthreads();
   if (tid == 0) {
     const uint32_t bytes = (uint32_t)ld * 4u;
     mbar_arrive_expect_tx(bar, 2u * bytes);
     tma_load_1d(row, c.tau + (size_t)j * ld, bytes, bar);
     tma_load_1d(erow, c.eta + (size_t)j * ld, bytes, bar);
-    *flag = mbar_wait_bounded(bar, 0, c.st) ? 1 : 0;
   }
+  if (tier) {  // the row itself, its k candidates and its tier, while the row lands
+    const size_t koff = (size_t)j * c.ldk;
+    for (int r = tid; r <= c.K + c.t2; r += nthreads) {
+      const int id = r < c.K ? c.nn[koff + r]
+                             : (r < c.K + c.t2 ? c.nn2[(size_t)j * kTier2 + (r - c.K)] : j);
+      if ((unsigned)id < (unsigned)n) atomicOr(&nbm[id >> 5], 1u << (id & 31));
+    }
+  }
+  if (tid == 0) *flag = mbar_wait_bounded(bar, 0, c.st) ? 1 : 0;
   __syncthreads();
   if (!*flag) return;
 
@@ -156,6 +172,7 @@ __device__ __forceinline__ void pheromone_row_body(const ColonyDev &c, const int
 
   float *trow = c.tau + (size_t)j * ld;
   float *crow = c.choice + (size_t)j * ld;
+  float mx = -1.0f;  // tier: largest choice value outside the marked cities
   for (int h4 = tid; h4 < ld / 4; h4 += nthreads) {
     const float4 t = reinterpret_cast<const float4 *>(row)[h4];
     const float4 e = reinterpret_cast<const float4 *>(erow)[h4];
@@ -166,6 +183,30 @@ __device__ __forceinline__ void pheromone_row_body(const ColonyDev &c, const int
     cv.z = choice_of(t.z, e.z, c.use_alpha, c.alpha);
     cv.w = choice_of(t.w, e.w, c.use_alpha, c.alpha);
     reinterpret_cast<float4 *>(crow)[h4] = cv;
+    if (tier) {
+      const int h = 4 * h4;  // four cities of one bitmap word
+      const uint32_t marked = nbm[h >> 5] >> (h & 31);
+      if (h + 0 < n && !(marked & 1u)) mx = fmaxf(mx, cv.x);
+      if (h + 1 < n && !(marked & 2u)) mx = fmaxf(mx, cv.y);
+      if (h + 2 < n && !(marked & 4u)) mx = fmaxf(mx, cv.z);
+      if (h + 3 < n && !(marked & 8u)) mx = fmaxf(mx, cv.w);
+    }
+  }
+  if (tier) {
+    for (int e = tid; e < c.t2; e += nthreads) {
+      const int id = c.nn2[(size_t)j * kTier2 + e];
+      c.t2v[(size_t)j * kTier2 + e] =
+          (unsigned)id < (unsigned)n ? choice_of(row[id], erow[id], c.use_alpha, c.alpha) : -1.0f;
+    }
+    for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    __syncthreads();  // dl is free again (the deposit fold used it)
+    if ((tid & 31) == 0) dl[tid >> 5] = mx;
+    __syncthreads();
+    if (tid < 32) {
+      float v = tid < (nthreads >> 5) ? dl[tid] : -1.0f;
+      for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+      if (tid == 0) c.mout[j] = v;
+    }
   }
   const size_t koff = (size_t)j * c.ldk;
   for (int r = tid; r < c.ldk; r += nthreads) {
@@ -201,7 +242,8 @@ __global__ void __launch_bounds__(512) k_batch_pheromone_rows(const ColonyDev *d
 }
 
 static size_t rows_smem(int ld, bool deposit) {
-  return (size_t)ld * 4 * (deposit ? 3 : 2) + (deposit ? 2 * kDepSeg * 12 : 0) + 32 * 4 + 16;
+  return (size_t)ld * 4 * (deposit ? 3 : 2) + (deposit ? 2 * kDepSeg * 12 : 0) + 32 * 4 + 16 +
+         (size_t)(ld / 32) * 4;
 }
 
 // At least two warps: warp 0 folds the deposits, the others stage them.

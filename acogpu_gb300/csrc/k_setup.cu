@@ -149,7 +149,8 @@ constexpr int kSortPerThread = kMaxSortRow / kSortThreads;
 
 __global__ void __launch_bounds__(kSortThreads)
     k_nn_sort_stable(const int32_t *__restrict__ dist, int n, int ld, int K, int ldk,
-                     int32_t *__restrict__ nn, int P, ColonyState *st) {
+                     int32_t *__restrict__ nn, int32_t *__restrict__ nn2, int t2, int P,
+                     ColonyState *st) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *keys = reinterpret_cast<uint64_t *>(smem);
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)P * 8);
@@ -201,10 +202,15 @@ __global__ void __launch_bounds__(kSortThreads)
   }
   for (int q = tid; q < ldk; q += kSortThreads)
     nn[(size_t)row * ldk + q] = q < K ? (int32_t)(uint32_t)(keys[q] & 0xffffffffu) : -1;
+  if (nn2)  // the fallback's second tier: neighbours K .. K + t2 - 1
+    for (int q = tid; q < kTier2; q += kSortThreads)
+      nn2[(size_t)row * kTier2 + q] =
+          q < t2 ? (int32_t)(uint32_t)(keys[K + q] & 0xffffffffu) : -1;
 }
 
 cudaError_t launch_nn_sort_stable(const int32_t *dist, int n, int ld, int K, int ldk, int32_t *nn,
-                                  ColonyState *st, cudaStream_t s) {
+                                  ColonyState *st, cudaStream_t s, int32_t *nn2, int t2) {
+  if (nn2 && (t2 < 0 || t2 > kTier2 || K + t2 > n - 1)) return cudaErrorInvalidValue;
   if (n > kMaxSortRow) return cudaErrorInvalidValue;
   int P = 1;
   while (P < n) P <<= 1;
@@ -213,7 +219,7 @@ cudaError_t launch_nn_sort_stable(const int32_t *dist, int n, int ld, int K, int
   cudaError_t e = cudaFuncSetAttribute(k_nn_sort_stable,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_nn_sort_stable<<<n, kSortThreads, smem, s>>>(dist, n, ld, K, ldk, nn, P, st);
+  k_nn_sort_stable<<<n, kSortThreads, smem, s>>>(dist, n, ld, K, ldk, nn, nn2, t2, P, st);
   return cudaGetLastError();
 }
 

@@ -87,6 +87,18 @@ enum aco_fallback {
                                  lowest index on ties (choose_best_next of ACOTSP) */
 };
 
+/* Second tier of the best-choice fallback (k <= 32): the next 128 nearest
+ * neighbours' choice values and the row's largest value outside them, written
+ * by the pheromone pass, settle most fallbacks without a scan of the row (same
+ * results either way).  It pays while the pheromone is spread over many
+ * edges (the Ant System) and not when a few reinforced edges hold it (the
+ * rank-based system after convergence). */
+enum aco_fallback_tier {
+  ACO_FALLBACK_TIER_AUTO = 0, /* on for ACO_ANT_SYSTEM, off for ACO_RANK_BASED */
+  ACO_FALLBACK_TIER_ON = 1,
+  ACO_FALLBACK_TIER_OFF = 2
+};
+
 enum aco_deposit_mode {
   ACO_DEPOSIT_DETERMINISTIC = 0, /* row-owned ordered fold: bit-exact with the
                                     reference's sequential CPU update */
@@ -154,7 +166,8 @@ typedef struct aco_params {
   uint64_t seed;     /* seed of the injected uniform stream (acogpu_rng.h) */
   int32_t ants_per_block; /* construction warps per CTA; 0 = tuned default */
   int32_t construct_mode; /* enum aco_construct_mode */
-  int32_t reserved[6];
+  int32_t fallback_tier;  /* enum aco_fallback_tier */
+  int32_t reserved[5];
 } aco_params;
 
 /* Reference defaults (inc/default.h, src/Colony.cu:31-36): AS, m = 10,

@@ -203,6 +203,26 @@ def test_coincident_cities_match_oracle(mode):
     run_pair(p, d, 3, ctx=f"coincident mode{mode}")
 
 
+@pytest.mark.parametrize("tier", [_abi.ACO_FALLBACK_TIER_ON, _abi.ACO_FALLBACK_TIER_OFF])
+@pytest.mark.parametrize("n,mode,variant,aging", [
+    (600, _abi.ACO_CONSTRUCT_STAGED, _abi.ACO_ANT_SYSTEM, 0),
+    (600, _abi.ACO_CONSTRUCT_STAGED, _abi.ACO_RANK_BASED, 1),
+    (2500, _abi.ACO_CONSTRUCT_CLUSTER, _abi.ACO_RANK_BASED, 0),
+])
+def test_fallback_tier_matches_oracle(tier, n, mode, variant, aging):
+    """The best-choice fallback with its second tier (the next 128 neighbours
+    and the row's largest choice value outside them) forced on or off, with
+    8 candidates so that many steps fall back: the same tours as the
+    oracle's scan of the whole row, through convergence."""
+    _, _, d = instance(n, 17 + n, kind="clustered")
+    p = params(num_ants=64, beta=2.0, rho=0.2, cand_k=8, seed=17, variant=variant, rank_w=6,
+               aging=aging, construct_mode=mode, fallback_tier=tier, **FAST_MODE)
+    if aging:
+        (p.min_retirement_age, p.max_retirement_age, p.global_performance,
+         p.min_population_limit) = (3, 6, 2, 40)
+    run_pair(p, d, 25 if n <= 1000 else 6, ctx=f"tier{tier} n{n}")
+
+
 def test_cluster_kernel_many_ants_matches_oracle():
     """The cluster kernel with several ant warps per CTA and more ants than
     one pass of the grid holds (n=2100: clusters of 3)."""
