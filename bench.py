@@ -406,7 +406,7 @@ def run_batch(args, rank, world, local):
 
 def run_large(args, rank, world, local):
     """Large single instance: n=4096 uniform in [0,100000)^2, m=512, k=32,
-    atomic deposit, plain AS (configs[2])."""
+    atomic deposit, plain AS (the cluster construction kernel)."""
     import torch
     import acogpu_gb300 as aco
     from acogpu_gb300 import _abi, instances

@@ -223,6 +223,17 @@ def test_fallback_tier_matches_oracle(tier, n, mode, variant, aging):
     run_pair(p, d, 25 if n <= 1000 else 6, ctx=f"tier{tier} n{n}")
 
 
+@pytest.mark.parametrize("n,k", [(45, 16), (31, 30), (160, 30), (700, 1)])
+def test_fallback_tier_edges_match_oracle(n, k):
+    """The second tier at its edges: shorter than 128 neighbours (n = 45,
+    k = 16: 28; n = 160), empty (n = 31, k = 30), and a single candidate
+    (every step but one falls back)."""
+    _, _, d = instance(n, 5 + n, kind="clustered")
+    p = params(num_ants=48, beta=2.0, rho=0.2, cand_k=k, seed=5 + n,
+               fallback_tier=_abi.ACO_FALLBACK_TIER_ON, **FAST_MODE)
+    run_pair(p, d, 8, ctx=f"tier edges n{n} k{k}")
+
+
 def test_cluster_kernel_many_ants_matches_oracle():
     """The cluster kernel with several ant warps per CTA and more ants than
     one pass of the grid holds (n=2100: clusters of 3)."""
