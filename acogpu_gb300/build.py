@@ -68,7 +68,7 @@ def build(force=False, verbose=False, extra_flags=()):
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-Xlinker", "--exclude-libs,ALL"]
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-ldl", "-Xlinker", "--exclude-libs,ALL"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

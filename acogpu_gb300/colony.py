@@ -78,6 +78,9 @@ def lib():
     L.aco_colony_set_stream.argtypes = [_vp, _vp]
     L.aco_colony_get_stats.argtypes = [_vp, ctypes.POINTER(_abi.AcoStats)]
     L.aco_colony_last_error.argtypes = [_vp]
+    L.aco_selftest_bounded_wait.argtypes = [ctypes.c_uint32]
+    L.aco_debug_fail_allocation.argtypes = [ctypes.c_int32]
+    L.aco_debug_fail_allocation.restype = None
     L.aco_colony_last_error.restype = ctypes.c_char_p
     L.aco_status_string.argtypes = [ctypes.c_int]
     L.aco_status_string.restype = ctypes.c_char_p

@@ -153,8 +153,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // the colony state and returns false.  No trap, no endless spin.
 constexpr uint32_t kMaxPolls = 1u << 22;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
-                                                  ColonyState *st) {
-  for (uint32_t i = 0; i < kMaxPolls; i++)
+                                                  ColonyState *st, uint32_t polls = kMaxPolls) {
+  for (uint32_t i = 0; i < polls; i++)
     if (mbar_try_wait(bar, parity)) return true;
   atomicOr(&st->error, kErrTimeout);
   return false;

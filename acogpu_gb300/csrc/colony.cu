@@ -10,7 +10,10 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
+#include <atomic>
 #include <new>
 #include <string>
 #include <vector>
@@ -26,6 +29,13 @@ namespace {
 
 const char *kNameAS = "Ant System";             // src/AntSystem.cu:7
 const char *kNameRBAS = "Rank-based Ant System";  // src/RankBasedAntSystem.cu:10
+
+// NVTX range over an API call: named in a profiler's timeline (nsys), a
+// no-op without one attached.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 int fail(aco_colony *c, int status, const std::string &msg) {
   if (c) c->err = msg;
@@ -44,8 +54,16 @@ int cuda_fail(aco_colony *c, cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
   } while (0)
 
+// Fault injection on the host: the `g_fail_alloc`-th next device allocation
+// of a colony reports out-of-memory without allocating (-1: off).
+std::atomic<int> g_fail_alloc{-1};
+
 template <class T>
 int dalloc(aco_colony *c, T **ptr, size_t count) {
+  int k = g_fail_alloc.load();
+  while (k >= 0 && !g_fail_alloc.compare_exchange_weak(k, k - 1)) {
+  }
+  if (k == 0) return fail(c, ACO_ERR_OUT_OF_MEMORY, "cudaMalloc: injected allocation failure");
   void *p = nullptr;
   cudaError_t e = cudaMalloc(&p, count * sizeof(T) + 16);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
@@ -344,6 +362,8 @@ int read_matrix_f32(aco_colony *c, const float *src, int cols, int ldsrc, float 
 
 extern "C" {
 
+void aco_debug_fail_allocation(int32_t after) { g_fail_alloc.store(after < 0 ? -1 : after); }
+
 void aco_params_default(aco_params *p) {
   if (!p) return;
   memset(p, 0, sizeof(*p));
@@ -428,6 +448,7 @@ int aco_colony_create_coords(const aco_params *params, const float *x, const flo
 }
 
 int aco_colony_initialize(aco_colony *c) {
+  NvtxRange range("aco_colony_initialize");
   if (c) state_changed(c);
   if (!c) return ACO_ERR_INVALID_ARGUMENT;
   drop_graph(c);
@@ -518,6 +539,7 @@ int aco_colony_initialize(aco_colony *c) {
 }
 
 int aco_colony_construct_solution(aco_colony *c, float *timers_ms) {
+  NvtxRange range("aco_colony_construct_solution");
   if (!c) return ACO_ERR_INVALID_ARGUMENT;
   if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
   state_changed(c);
@@ -557,6 +579,7 @@ int aco_colony_construct_solution(aco_colony *c, float *timers_ms) {
 }
 
 int aco_colony_run(aco_colony *c, int32_t iterations) {
+  NvtxRange range("aco_colony_run");
   if (!c || iterations < 0) return ACO_ERR_INVALID_ARGUMENT;
   state_changed(c);
   if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
@@ -1040,6 +1063,7 @@ int aco_batch_create(const aco_params *params, int32_t count, const int32_t *siz
 }
 
 int aco_batch_initialize(aco_batch *b) {
+  NvtxRange range("aco_batch_initialize");
   if (!b) return ACO_ERR_INVALID_ARGUMENT;
   b->initialized = false;
   batch_drop_graph(b);
@@ -1068,6 +1092,7 @@ int aco_batch_initialize(aco_batch *b) {
 }
 
 int aco_batch_run(aco_batch *b, int32_t iterations) {
+  NvtxRange range("aco_batch_run");
   if (!b || iterations < 0) return ACO_ERR_INVALID_ARGUMENT;
   if (!b->initialized) return bfail(b, ACO_ERR_NOT_INITIALIZED, "batch not initialized");
   for (aco_colony *c : b->cols) state_changed(c);  // the replays rewrite every state block

@@ -483,6 +483,24 @@ ACO_API const float *aco_tsplib_ycoords(const aco_tsplib *t);
 ACO_API const char *aco_tsplib_last_error(void);
 ACO_API void aco_tsplib_destroy(aco_tsplib *t);
 
+/* ---- failure path self-tests ---------------------------------------------
+ * The reference exits on every CUDA error (inc/helper_cuda.h:316-325); here
+ * every entry point returns a status and every device-side wait is bounded.
+ * These two calls exercise those paths without faulting or hanging a GPU.
+ *
+ * aco_selftest_bounded_wait: one kernel waits on an mbarrier that nothing
+ * arrives on, gives up after `polls` polls (1 .. 2^22), records the timeout
+ * as the engine's kernels do, and exits normally.  Returns
+ * ACO_ERR_DEVICE_TIMEOUT -- the expected outcome -- once the kernel has
+ * finished and the flag has been read back; ACO_ERR_CUDA if the launch or
+ * the copy failed.  The CUDA context stays usable.
+ *
+ * aco_debug_fail_allocation: the after-th next device allocation made by a
+ * colony (0 = the next one) reports ACO_ERR_OUT_OF_MEMORY without
+ * allocating; a negative value switches the injection off.  Process-wide. */
+ACO_API int aco_selftest_bounded_wait(uint32_t polls);
+ACO_API void aco_debug_fail_allocation(int32_t after);
+
 #ifdef __cplusplus
 }
 #endif
