@@ -497,7 +497,8 @@ int aco_colony_initialize(aco_colony *c) {
     int32_t *scratch = nullptr, *full = nullptr;
     ACO_CUDA(c, cudaMallocAsync(&scratch, (size_t)n * c->ld * 4, c->stream), "alloc scratch");
     if (c->K == n) {
-      full = c->nn;
+      full = c->nn;  // the sort writes n ids a row; the pitch's padding is -1
+      ACO_CUDA(c, cudaMemsetAsync(c->nn, 0xff, (size_t)n * c->ldk * 4, c->stream), "memset nn");
     } else {
       ACO_CUDA(c, cudaMallocAsync(&full, (size_t)n * c->ld * 4, c->stream), "alloc scratch");
     }

@@ -750,7 +750,7 @@ __device__ __forceinline__ int staged_steps(const ColonyDev &c, int k, uint32_t 
             if (next < 0) next = fallback_best_reg<TW, WIDE, FB>(c, cur, tw, a, lane);
           }
         } else {  // select_local_best on a full row of at most 32 cities (k == n)
-          const unsigned um = __ballot_sync(kFull, id >= 0 && !vis);
+          const unsigned um = __ballot_sync(kFull, lane < c.K && id >= 0 && !vis);
           next = um ? __shfl_sync(kFull, id, 31 - __clz(um)) : -1;
         }
         fallbacks += hit == 0u;

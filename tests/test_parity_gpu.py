@@ -234,6 +234,20 @@ def test_fallback_tier_edges_match_oracle(n, k):
     run_pair(p, d, 8, ctx=f"tier edges n{n} k{k}")
 
 
+@pytest.mark.parametrize("n", [8, 22, 31])
+@pytest.mark.parametrize("order", [_abi.ACO_NN_REFERENCE_QSORT, _abi.ACO_NN_STABLE])
+def test_small_full_rows_match_oracle(n, order):
+    """Full rows of at most 32 cities (k = n) on the staged kernel, with the
+    reference fallback (the last unvisited city of the row): the rows' padding
+    past n must never be taken for a city (a defect found by a randomized
+    sweep: the reference-order sort left it unset)."""
+    _, _, d = instance(n, 300 + n)
+    p = params(num_ants=3 * n, beta=2.0, rho=0.2, cand_k=0, seed=300 + n, nn_order=order,
+               heuristic=_abi.ACO_HEURISTIC_DEVICE, fallback=_abi.ACO_FALLBACK_REFERENCE,
+               tau0_mode=_abi.ACO_TAU0_DORIGO)
+    run_pair(p, d, 6, ctx=f"full row n{n} order{order}")
+
+
 def test_cluster_kernel_many_ants_matches_oracle():
     """The cluster kernel with several ant warps per CTA and more ants than
     one pass of the grid holds (n=2100: clusters of 3)."""
