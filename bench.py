@@ -373,6 +373,7 @@ def run_batch(args, rank, world, local):
     b.run(args.warmup)
     b.synchronize()
     built0, launches0 = b.tours_built(), b.launch_count()
+    fb0 = np.array([b.colony(i).stats()["fallbacks"] for i in range(len(insts))], np.float64)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
@@ -386,6 +387,17 @@ def run_batch(args, rank, world, local):
     launches = b.launch_count() - launches0
     sizes = np.array([len(x) for x, _ in allinst])
     ants = np.minimum(sizes, BATCH_CAP)
+    # Roofline of the construction kernel on this GPU's shard: the bytes of
+    # construct_bytes per instance (its fallbacks counted over the timed
+    # steps) over the autotuner's event-timed construction launch.
+    fb1 = np.array([b.colony(i).stats()["fallbacks"] for i in range(len(insts))], np.float64)
+    my_n = np.array([len(x) for x, _ in insts], np.float64)
+    my_m = np.minimum(my_n, BATCH_CAP)
+    my_k = np.minimum(BATCH_K, my_n - 1)
+    bytes_c = float((my_m * (my_n - 1) * (8 * my_k + 8)).sum() +
+                    ((fb1 - fb0) / args.steps * 4 * my_n).sum())
+    hbm = peaks().get("hbm_gbs")
+    achieved = bytes_c / (tune["construct_ms"] / 1e3) / 1e9
     best = b.glob_best()
     b.close()
     (dev_s,), (tours, launches, best_sum) = distrib.reduce_times_and_counts(
@@ -401,6 +413,11 @@ def run_batch(args, rank, world, local):
                        "l2": "working set 5+ GB, larger than L2"},
             "ant_steps_per_s": float((ants * (sizes - 1)).sum()) * args.steps / dev_s,
             "autotune": tune, "setup_s": setup_s, "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "k_batch_construct", "achieved": achieved,
+                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm else None,
+                         "algorithmic_bytes_per_launch": bytes_c, "traffic": None,
+                         "traffic_source": "not captured: the batch holds 5+ GB on the device"},
             "mean_best_length": best_sum / len(allinst), "clocks": clk.summary()}
 
 
