@@ -91,6 +91,42 @@ def test_port_matches_compiled_reference(n, m, aging, stable, beta, rho, iters, 
 
 
 @needs_ref
+@pytest.mark.parametrize("stable", [False, True])
+def test_port_matches_compiled_reference_with_coincident_cities(stable):
+    """Cities moved onto one point in triples: distance 0, an infinite
+    heuristic and choice value, row sums of +inf.  The reference's walk then
+    runs past the row into select_local_best (or stops at the first
+    candidate for u*S = NaN); the port must follow it exactly -- this pins
+    the engine's handling of infinite weights to the reference itself."""
+    from acogpu_gb300 import instances
+    n, m = 48, 24
+    x, y = instances.uniform_instance(n, seed=77)
+    x, y = np.array(x), np.array(y)
+    pick = np.random.default_rng(77).choice(n, 12, replace=False).reshape(4, 3)
+    for a, b, c in pick:
+        x[b] = x[c] = x[a]
+        y[b] = y[c] = y[a]
+    d = instances.euc2d_distances(x, y)
+    assert (d[~np.eye(n, dtype=bool)] == 0).sum() >= 24
+    p = params(num_ants=m, beta=2.0, rho=0.2, seed=77,
+               nn_order=_abi.ACO_NN_STABLE if stable else _abi.ACO_NN_REFERENCE_QSORT)
+    ref = oracle.Ref(p, d, stable_nn=stable)
+    ref.initialize()
+    q = oracle.Port(p, d, threads=3)
+    q.initialize()
+    assert np.isinf(q.heuristic()).any()
+    for it in range(8):
+        ref.iterate()
+        q.iterate()
+        assert np.array_equal(ref.tours(), q.tours()), it
+        assert np.array_equal(ref.lengths(), q.lengths()), it
+        assert np.array_equal(bits(ref.pheromone()), bits(q.pheromone())), it
+        assert (ref.iter_best(), ref.glob_best()) == (q.iter_best(), q.glob_best())
+    ref.close()
+    q.close()
+
+
+@needs_ref
 def test_reference_quicksort_order_differs_from_stable():
     """Ties in rounded distances make the reference's quicksort order differ
     from the stable order; both orders are reproduced."""
