@@ -324,6 +324,10 @@ class Ref:
         if self.h:
             self.L.acoref_destroy(self.h)
             self.h = None
+        # The reference prints diagnostics through C stdio ("probability
+        # issue" when its walk runs past a row); flush them now, while the
+        # caller's output capture is still in place.
+        ctypes.CDLL(None).fflush(None)
 
     def __del__(self):
         try:
