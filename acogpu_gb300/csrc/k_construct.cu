@@ -98,8 +98,12 @@ cudaError_t launch_aging_plan(const ColonyDev &c, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// Shared-memory layout of the staged kernel: the table of staged_layout,
-// then per warp 32 f32, then the mbarrier.  G = pitch / 4.
+// Staged kernel (k <= 32 and a candidate table that fits in shared memory,
+// e.g. n = 1000, k = 30: 192 KB): each CTA copies the whole table -- int16
+// ids and FP32 choice values at pitch 4G -- into shared memory with TMA bulk
+// copies once per launch, so a construction step touches only shared memory.
+// One CTA per SM; its warps loop over ants.  Shared-memory layout: the table
+// of staged_layout, then per warp 32 f32, then the mbarrier.
 //
 // Without aging every CTA stages the table and its warps build tours.  With
 // aging the ants' roles come from k_aging_plan: CTA b < B takes blend ant b

@@ -1,43 +1,37 @@
-// k_construct_steps.cuh -- device code shared by the construction kernels
-// (k_construct.cu: general, staged and direct; k_construct_cluster.cu;
-// k_construct_batch.cu).
-//
+// k_construct_steps.cuh -- roulette-wheel tour construction, one warp per
+// ant: the device code shared by the construction kernels (k_construct.cu:
+// general, staged and direct; k_construct_cluster.cu; k_construct_batch.cu).
 //
 // Replaces Colony::initTour + constructPath (src/Colony.cu:469-527,
 // 689-864) and the reference GPU kernels dev_place_ants /
 // dev_compute_probabilities / dev_reduce_probabilities_s / dev_move_ants
 // (inc/Colony.cuh:136-162,193-229,290-347; src/Colony.cu:643-685), which the
 // reference launches 3(n-1) times per iteration with a device sync after
-// each.  Here one launch builds every tour:
+// each.  Here one launch builds every tour.  Two step loops:
 //
-//  * the tabu list is a bitmask in shared memory (n bits per warp);
-//  * step x of ant k reads the candidate row of the current city in
-//    candidate order (ids + tau*eta, contiguous), masks visited cities and
-//    forms the prefix sums of the weights in candidate order.  The prefix is
-//    the sequential float sum of the reference (sum_prob += prob_ptr[i],
-//    src/Colony.cu:814; partial_sum += ..., :840): the non-zero weights of a
-//    chunk are compacted by ballot and added in lane order, so every partial
-//    sum is bit-identical to the CPU's (the zero weight of a visited city
-//    changes no sum);
-//  * the crossing `first i with partial_sum > u * sum` is a ballot; rows
-//    longer than 32 candidates keep the prefix at each chunk end in shared
-//    memory and redo only the chunk that holds the crossing;
-//  * when the roulette cannot pick (sum <= 0, or no crossing) the fallback is
-//    a ballot over the row: the last unvisited city of the full nn row
-//    (select_local_best, inc/Colony.cuh:33-43) or the unvisited city with the
-//    largest choice value;
-//  * ant aging (updateAntAges, src/Colony.cu:353-364; compute_fittness,
-//    inc/Colony.cuh:14-31) is fused in; the integer tour length (the
-//    reference adds it per move, inc/Colony.cuh:337-340) is summed by the
-//    whole warp after the tour is built, so no step waits on a distance load;
-//    the successor/predecessor of every city is written transposed for the
-//    row-owned deposit.
+//  * construct_ant (any k, full rows included): the tabu list is a bitmask
+//    in shared memory; the non-zero weights of each 32-candidate chunk are
+//    compacted by ballot and folded in lane order, so every partial sum is
+//    the reference's sequential float sum (sum_prob += prob_ptr[i],
+//    src/Colony.cu:814; partial_sum += ..., :840); rows longer than 32 keep
+//    the prefix at each chunk end and redo only the chunk of the crossing;
+//  * staged_steps (k <= 32; the staged, cluster, direct and batch kernels):
+//    the tabu list in registers, lane r holding candidate r of the current
+//    row, every lane's prefix formed by masked FMAs (see staged_steps), the
+//    rows read through a policy (TableRows: shared or global memory;
+//    ClusterRows: distributed shared memory of a thread-block cluster).
 //
-// Staged variant (candidate lists of at most 32 and a table that fits in
-// shared memory, e.g. n = 1000, k = 30: 192 KB): each CTA copies the whole
-// candidate table -- int16 ids and FP32 choice values, 32 per city -- into
-// shared memory with TMA bulk copies once per launch, so a construction step
-// touches only shared memory.  One CTA per SM; its warps loop over ants.
+// In both, the crossing `first i with partial_sum > u * sum` is a ballot;
+// when the roulette cannot pick (sum <= 0, or no crossing) the fallback is
+// the last unvisited city of the full nn row (select_local_best,
+// inc/Colony.cuh:33-43) or the unvisited city with the largest choice value
+// (through the second tier where the colony keeps one, see fallback_tier2).
+// Ant aging (updateAntAges, src/Colony.cu:353-364; compute_fittness,
+// inc/Colony.cuh:14-31) is fused in; the integer tour length (the reference
+// adds it per move, inc/Colony.cuh:337-340) is summed by the whole warp after
+// the tour is built, so no step waits on a distance load; the
+// successor/predecessor of every city is written transposed for the
+// row-owned deposit.
 #pragma once
 #include <cuda_runtime.h>
 
