@@ -13,7 +13,11 @@ namespace aco {
 // (mapa + ld.shared::cluster) with the staged step loop; a second barrier
 // keeps each slice alive until the whole cluster is done.  Every thread
 // reaches both barriers on every path (a copy that timed out only records
-// the error).  All CTAs share all ants.
+// the error, and the ants run only when every rank staged its slice).  All
+// CTAs share all ants.  Launches of at most kWideFallbackWarps warps use the
+// FB = 16 instantiation (255 registers a thread: the fallback's full-row scan
+// keeps 16 row chunks in flight); the fallback is a called function here
+// (ClusterRows::kOutlineFallback), which keeps the step loop small.
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
