@@ -308,7 +308,9 @@ int plan_construction(aco_colony *c) {
     const int cs = (c->n + 1023) / 1024;
     int clusters = 0;
     const ColonyDev d = make_dev(c);
-    if (cs >= 2 && cs <= 8) {
+    // A table of at most 1024 rows fits one CTA (the staged kernel); a
+    // cluster of one is taken only when asked for.
+    if (cs >= (mode == ACO_CONSTRUCT_CLUSTER ? 1 : 2) && cs <= 8) {
       // warps per CTA for the ants over the CTAs that fit, one pass
       int w = (c->m + sms - 1) / sms;
       w = w < 1 ? 1 : (w > kStagedMaxWarps ? kStagedMaxWarps : w);

@@ -157,13 +157,13 @@ def test_staged_blend_ants_match_oracle(m, six, iters):
 
 
 @pytest.mark.parametrize("mode", ["direct", "cluster"])
-@pytest.mark.parametrize("n,k,aging", [(1500, 32, 0), (3000, 20, 1), (5000, 32, 0),
-                                       (8192, 16, 0)])
+@pytest.mark.parametrize("n,k,aging", [(700, 24, 1), (1500, 32, 0), (3000, 20, 1),
+                                       (5000, 32, 0), (8192, 16, 0)])
 def test_large_table_kernels_match_oracle(n, k, aging, mode):
     """k <= 32 with a candidate table too large for one CTA's shared memory:
     the step loop on rows read from L2 (direct) or on the table split over a
     cluster of ceil(n/1024) CTAs read through distributed shared memory
-    (cluster: 2, 3, 5 and 8 CTAs), with the tabu list in 2, 4, 8 and 8
+    (cluster: 1, 2, 3, 5 and 8 CTAs), with the tabu list in 2, 2, 4, 8 and 8
     registers per lane, reproduces the oracle (aging: through the blend and
     its fallback)."""
     _, _, d = instance(n, 50 + n, kind="clustered")
