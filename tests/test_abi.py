@@ -52,3 +52,44 @@ def test_status_strings_and_invalid_arguments():
     d = np.zeros((10, 10), np.int32)
     assert L.aco_colony_create(ctypes.byref(p), d.ctypes.data_as(ctypes.c_void_p), 10, 0,
                                ctypes.byref(h)) == _abi.ACO_ERR_UNSUPPORTED
+
+
+def header_enums():
+    src = open(os.path.join(ROOT, "include", "acogpu.h")).read()
+    return {k: int(v) for k, v in re.findall(r"\b(ACO_[A-Z0-9_]+)\s*=\s*(-?\d+)", src)}
+
+
+def test_enum_constants_match_the_python_mirror():
+    consts = header_enums()
+    assert len(consts) >= 40
+    mirrored = {k: v for k, v in consts.items() if hasattr(_abi, k)}
+    wrong = {k: (v, getattr(_abi, k)) for k, v in mirrored.items() if getattr(_abi, k) != v}
+    assert not wrong, wrong
+    for k in ("ACO_CONSTRUCT_DIRECT", "ACO_CONSTRUCT_CLUSTER", "ACO_FALLBACK_TIER_AUTO",
+              "ACO_FALLBACK_TIER_ON", "ACO_FALLBACK_TIER_OFF", "ACO_ERR_DEVICE_TIMEOUT"):
+        assert k in mirrored, k
+
+
+def test_params_field_order_matches_the_header():
+    src = open(os.path.join(ROOT, "include", "acogpu.h")).read()
+    body = src[src.index("typedef struct aco_params {"):src.index("} aco_params;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = re.findall(r"^\s*(?:int32_t|uint64_t|float)\s+(\w+)", body, flags=re.M)
+    assert names == [f for f, _ in _abi.AcoParams._fields_], names
+
+
+def test_mode_values_are_checked_before_any_device_call():
+    L = aco.lib()
+    h = ctypes.c_void_p()
+    d = np.zeros((40, 40), np.int32)
+    ptr = d.ctypes.data_as(ctypes.c_void_p)
+    for field, bad in (("construct_mode", 5), ("construct_mode", -1), ("fallback_tier", 3)):
+        p = _abi.default_params(cand_k=20, fallback=_abi.ACO_FALLBACK_BEST)
+        setattr(p, field, bad)
+        assert L.aco_colony_create(ctypes.byref(p), ptr, 40, 0, ctypes.byref(h)) == \
+            _abi.ACO_ERR_INVALID_ARGUMENT, (field, bad)
+    # the k <= 32 kernels, forced with a longer candidate list or the full row
+    for mode in (_abi.ACO_CONSTRUCT_STAGED, _abi.ACO_CONSTRUCT_DIRECT, _abi.ACO_CONSTRUCT_CLUSTER):
+        p = _abi.default_params(cand_k=0, construct_mode=mode)
+        assert L.aco_colony_create(ctypes.byref(p), ptr, 40, 0, ctypes.byref(h)) == \
+            _abi.ACO_ERR_UNSUPPORTED, mode
