@@ -455,10 +455,14 @@ def run_large(args, rank, world, local):
     best = col.getGlobBestDist()
     launches = col.launch_count() - l0
     col.close()
+    # N GPUs run independent replicas: the slowest rank's time, every rank's tours
+    (ms,), (tours_all,) = distrib.reduce_times_and_counts(
+        [ms], [tours], device=torch.device("cuda", local))
     if rank != 0:
         return None
-    return {"metric": "tours/s", "value": tours / (ms / 1e3), "unit": "tours/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+    return {"metric": "tours/s", "value": tours_all / (ms / 1e3), "unit": "tours/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": "plain AS, n=4096 uniform in [0,100000)^2, m=512, k=32, "
@@ -617,20 +621,19 @@ def main():
         import torch
         torch.cuda.set_device(local)
         torch.distributed.init_process_group("nccl")
-    if args.workload in ("batch512", "learned", "large4096"):
-        fn = {"batch512": run_batch, "learned": run_learned, "large4096": run_large}[args.workload]
+    try:
+        fn = {"batch512": run_batch, "learned": run_learned, "large4096": run_large,
+              "rbas_aging_n1000": run_ours}[args.workload]
         out = fn(args, rank, world, local)
         if out is not None:
+            # the CPU baseline: rank 0 of a one-GPU run only
+            if fn is run_ours and not args.no_cpu_baseline and world == 1:
+                out["cpu_baseline"] = cpu_baseline()
             print(json.dumps(out), flush=True)
-        return
-    out = run_ours(args, rank, world, local)
-    if out is not None:
-        if not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline()
-        print(json.dumps(out), flush=True)
-    if world > 1:
-        import torch
-        torch.distributed.destroy_process_group()
+    finally:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
 
 
 if __name__ == "__main__":
