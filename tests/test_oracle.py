@@ -91,8 +91,8 @@ def test_port_matches_compiled_reference(n, m, aging, stable, beta, rho, iters, 
 
 
 @needs_ref
-@pytest.mark.parametrize("stable", [False, True])
-def test_port_matches_compiled_reference_with_coincident_cities(stable):
+@pytest.mark.parametrize("stable,aging", [(False, 0), (True, 0), (False, 1)])
+def test_port_matches_compiled_reference_with_coincident_cities(stable, aging):
     """Cities moved onto one point in triples: distance 0, an infinite
     heuristic and choice value, row sums of +inf.  The reference's walk then
     runs past the row into select_local_best (or stops at the first
@@ -108,20 +108,27 @@ def test_port_matches_compiled_reference_with_coincident_cities(stable):
         y[b] = y[c] = y[a]
     d = instances.euc2d_distances(x, y)
     assert (d[~np.eye(n, dtype=bool)] == 0).sum() >= 24
-    p = params(num_ants=m, beta=2.0, rho=0.2, seed=77,
+    p = params(num_ants=m, beta=2.0, rho=0.2, seed=77, aging=aging,
                nn_order=_abi.ACO_NN_STABLE if stable else _abi.ACO_NN_REFERENCE_QSORT)
+    if aging:
+        (p.min_retirement_age, p.max_retirement_age, p.global_performance,
+         p.min_population_limit) = (3, 5, 2, m // 2)
     ref = oracle.Ref(p, d, stable_nn=stable)
     ref.initialize()
     q = oracle.Port(p, d, threads=3)
     q.initialize()
     assert np.isinf(q.heuristic()).any()
-    for it in range(8):
+    for it in range(12 if aging else 8):
         ref.iterate()
         q.iterate()
         assert np.array_equal(ref.tours(), q.tours()), it
         assert np.array_equal(ref.lengths(), q.lengths()), it
         assert np.array_equal(bits(ref.pheromone()), bits(q.pheromone())), it
         assert (ref.iter_best(), ref.glob_best()) == (q.iter_best(), q.glob_best())
+        if aging:
+            a, b = ref.aging_state(), q.aging()
+            for key in ("age", "perf", "valid"):
+                assert np.array_equal(a[key], b[key]), (it, key)
     ref.close()
     q.close()
 
