@@ -248,6 +248,29 @@ def test_small_full_rows_match_oracle(n, order):
     run_pair(p, d, 6, ctx=f"full row n{n} order{order}")
 
 
+@pytest.mark.parametrize("k", [0, 16])
+def test_subnormal_choice_values_match_oracle(k):
+    """beta = 5 on a 100000-wide box with tau0 = 1e-18: choice values down to
+    about 1e-44, below the smallest normal float (1.2e-38).  Nothing may flush
+    them to zero: the GPU follows the oracle's exact float arithmetic."""
+    x, y, d = instance(60, 91, box=100000)
+    p = params(num_ants=40, beta=5.0, rho=0.5, cand_k=k, seed=91,
+               tau0_mode=_abi.ACO_TAU0_VALUE, tau0=1e-18,
+               nn_order=_abi.ACO_NN_STABLE, heuristic=_abi.ACO_HEURISTIC_DEVICE,
+               fallback=_abi.ACO_FALLBACK_BEST if k else _abi.ACO_FALLBACK_REFERENCE)
+    g, q = pair(p, d)
+    ch = q.choice()
+    tiny = ch[(ch > 0) & (ch < np.float32(1.17549435e-38))]
+    assert tiny.size > 0  # the case really holds subnormal choice values
+    assert np.array_equal(bits(g.choice_info()), bits(ch))
+    for it in range(4):
+        g.constructSolution()
+        q.iterate()
+        assert_same_state(g, q, ctx=f"subnormal k{k} iteration {it}")
+    g.close()
+    q.close()
+
+
 def test_cluster_kernel_many_ants_matches_oracle():
     """The cluster kernel with several ant warps per CTA and more ants than
     one pass of the grid holds (n=2100: clusters of 3)."""
