@@ -381,29 +381,32 @@ ACO_API int aco_colony_read_candidate_heuristic(aco_colony *c, float *out_nk);
 /* Largest city count accepted by aco_nn_list_reference_order_noalloc. */
 #define ACO_NOALLOC_MAX_CITIES 1024
 
-/* nn-list build that allocates no device memory.  It has no counterpart in
- * the reference (whose computeNNlist, src/Colony.cu:276-311, runs inside
- * Colony::initialize); it exists for callers that cannot call cudaMalloc or
- * cudaFree -- code that must not trigger the device-wide synchronisation of
- * cudaFree while other streams run, code whose device memory belongs to a
- * framework allocator or a fixed budget, code that must not meet an
- * out-of-memory error midway.
+/* nn-list build that allocates no device memory.  This entry point has no
+ * counterpart in the reference.  It exists for callers that cannot call
+ * cudaMalloc or cudaFree: code that must not trigger the device-wide
+ * synchronisation of cudaFree while other streams run, code whose device
+ * memory belongs to a framework allocator or a fixed budget, code that must
+ * not meet an out-of-memory error midway.
  *
  *   dist_dev: n*n int32 distances in device memory (row-major, MAX on the
  *             diagonal); nn_dev: n*n int32 output in device memory, each row
- *             the cities sorted by distance in the order of the reference's
- *             CPU quicksort, ties included -- the same rows as a colony built
+ *             the cities sorted by distance, ties in the order of the
+ *             ACO_NN_REFERENCE_QSORT rule -- the same rows as a colony built
  *             with ACO_NN_REFERENCE_QSORT and full-row candidates.
  *   n: 1 <= n <= ACO_NOALLOC_MAX_CITIES, otherwise ACO_ERR_UNSUPPORTED.
- *   stream: cudaStream_t (NULL for the default stream); the call waits for
- *           its own work and returns the status.
+ *   stream: cudaStream_t (NULL for the default stream).  The call is
+ *           synchronous: it waits for its own work on the stream, reads the
+ *           kernel's error flags back, and returns the status.
  *
  * The sort's scratch is a fixed 4 MiB __device__ array inside the library,
- * held by every GPU that loads the library until the process exits.  The
- * first call on a device looks up that array's device address (with the
- * device current); make that first call before any stream capture.  All
- * calls share the one array: calls that overlap on the GPU (from several
- * host threads or streams at once) race and must not be issued. */
+ * held by every GPU that loads the library until the process exits.  Its
+ * device address is looked up once per CUDA context, with the device
+ * current: the first call on a device does this set-up (make that first
+ * call before any stream capture), and so does the first call after the
+ * device's context was replaced, e.g. by cudaDeviceReset.  All calls share
+ * the one array and the kernel's error flags: calls that overlap on the GPU
+ * (from several host threads or streams at once) race and must not be
+ * issued. */
 ACO_API int aco_nn_list_reference_order_noalloc(const int32_t *dist_dev, int32_t n,
                                                 int32_t *nn_dev, void *stream);
 

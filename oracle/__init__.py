@@ -21,7 +21,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libaco_oracle.so")
 REF_SO = {False: os.path.join(HERE, "_ref", "libacoref_noaging.so"),
           True: os.path.join(HERE, "_ref", "libacoref_aging.so")}
-REF_SOURCES = os.environ.get("ACO_REFERENCE_DIR", "/root/reference")
+# The reference checkout: ACO_REFERENCE_DIR, else a `reference` directory
+# beside this repository.  Absent on machines without it (the checks that
+# need it are skipped there).
+REF_SOURCES = (os.environ.get("ACO_REFERENCE_DIR")
+               or os.path.normpath(os.path.join(HERE, os.pardir, os.pardir, "reference")))
 
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)

@@ -1,7 +1,7 @@
 """Generate the golden fixtures from the reference's own CPU AntSystem.
 
-Run in a checkout that has the reference sources (default /root/reference,
-or ACO_REFERENCE_DIR): it builds oracle/_ref with oracle/Makefile, runs the
+Run in a checkout that has the reference sources (ACO_REFERENCE_DIR, or a
+`reference` directory beside this repository): it builds oracle/_ref with oracle/Makefile, runs the
 unmodified reference path with the injected random stream on small seeded
 instances and records, per iteration, the tours, lengths and best values and
 a hash of the pheromone matrix.  The fixtures pin the oracle and the GPU

@@ -9,11 +9,12 @@ import numpy as np
 import pytest
 
 import acogpu_gb300 as aco
+import oracle
 from acogpu_gb300.colony import LIB_PATH
 from helpers import instance
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("ACO_REFERENCE_DIR", "/root/reference")
+REF = oracle.REF_SOURCES
 
 
 def _compiler():

@@ -14,7 +14,7 @@ from acogpu_gb300 import _abi, instances
 from acogpu_gb300.colony import AcoError
 from acogpu_gb300 import tsplib
 
-REF = os.environ.get("ACO_REFERENCE_DIR", "/root/reference")
+REF = oracle.REF_SOURCES
 INPUT = os.path.join(REF, "release", "input")
 _libc = ctypes.CDLL(ctypes.util.find_library("c"))
 _libc.strtof.restype = ctypes.c_float
