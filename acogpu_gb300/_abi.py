@@ -27,6 +27,7 @@ ACO_DEPOSIT_DETERMINISTIC, ACO_DEPOSIT_ATOMIC = 0, 1
 ACO_TAU0_REFERENCE, ACO_TAU0_DORIGO, ACO_TAU0_VALUE = 0, 1, 2
 ACO_CONSTRUCT_AUTO, ACO_CONSTRUCT_GLOBAL, ACO_CONSTRUCT_STAGED = 0, 1, 2
 ACO_CONSTRUCT_DIRECT, ACO_CONSTRUCT_CLUSTER = 3, 4
+ACO_CONSTRUCT_ROWS = 5
 ACO_FALLBACK_TIER_AUTO, ACO_FALLBACK_TIER_ON, ACO_FALLBACK_TIER_OFF = 0, 1, 2
 ACO_GEMM_MMA_SYNC, ACO_GEMM_TCGEN05 = 0, 1
 

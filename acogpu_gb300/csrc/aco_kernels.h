@@ -68,6 +68,7 @@ cudaError_t launch_construct_staged(const ColonyDev &c, const int16_t *nn16, int
 // Aging colonies: the age update and the ants' roles that the staged kernel
 // reads (launched right before it).
 cudaError_t launch_aging_plan(const ColonyDev &c, cudaStream_t s);
+cudaError_t launch_batch_aging_plan(const ColonyDev *descs, int count, cudaStream_t s);
 // k <= 32, rows read from L2 by the staged step loop (n <= kDirectMaxCities).
 constexpr int kDirectMaxCities = 8192;
 cudaError_t launch_construct_direct(const ColonyDev &c, int grid, int warps, cudaStream_t s);
@@ -76,7 +77,49 @@ cudaError_t launch_construct_direct(const ColonyDev &c, int grid, int warps, cud
 cudaError_t query_construct_cluster(const ColonyDev &c, int warps, int cs, int *max_clusters);
 cudaError_t launch_construct_cluster(const ColonyDev &c, int grid, int warps, int cs,
                                      cudaStream_t s);
-cudaError_t launch_nn_to_i16(const int32_t *nn, int n, int ldk, int16_t *nn16, cudaStream_t s);
+// Long candidate rows (k > 32, full rows included; n <= kRowsMaxCities): a
+// CTA holds A <= kRowsMaxAnts ants of one instance, one scan warp per ant and
+// one chain warp (k_construct_rows.cu).  Each ant has a region of
+// rows_ant_bytes in shared memory (rows_layout): two buffers of compacted
+// weights and int32 ids (S = rows_slots(K) entries each), the running sums at
+// every 32nd entry, a staging area for one row copied by TMA (pitch P = ldk:
+// choice or tau, eta, int16 ids) and the tabu bits.  With aging,
+// launch_construct_rows runs the aging plan first (two launches).
+constexpr int kRowsMaxCities = 8192;
+constexpr int kRowsMaxAnts = 11;
+__host__ __device__ inline int rows_slots(int K) { return (K + 31) / 32 * 32 + 32; }
+struct RowsLayout {
+  int S;
+  size_t id_off, bend_off, sw_off, se_off, si_off, tw_off, bytes;
+};
+__host__ __device__ inline RowsLayout rows_layout(int n, int K, int P) {
+  RowsLayout L;
+  L.S = rows_slots(K);
+  L.id_off = (size_t)L.S * 8;
+  L.bend_off = (size_t)L.S * 16;
+  L.sw_off = L.bend_off + ((size_t)L.S / 32 * 4 + 15) / 16 * 16;
+  L.se_off = L.sw_off + (size_t)P * 4;
+  L.si_off = L.se_off + (size_t)P * 4;
+  L.tw_off = L.si_off + ((size_t)P * 2 + 15) / 16 * 16;
+  L.bytes = L.tw_off + (size_t)(((n + 31) / 32 + 3) / 4) * 16;
+  return L;
+}
+__host__ __device__ inline size_t rows_ant_bytes(int n, int K, int P) {
+  const size_t b = rows_layout(n, K, P).bytes;
+  return (b + 127) / 128 * 128 + 16;  // consecutive regions start four banks apart
+}
+cudaError_t configure_construct_rows(size_t smem);
+cudaError_t launch_construct_rows(const ColonyDev &c, int grid, int ants, cudaStream_t s);
+// max_ldk: the largest candidate-row pitch of the batch (every instance's
+// layout fits in rows_ant_bytes(max_n, max_ldk, max_ldk)).
+size_t batch_rows_smem_bytes(int max_n, int max_ldk, int ants);
+cudaError_t configure_batch_construct_rows(size_t smem);
+int batch_rows_blocks_per_sm(int ants, size_t smem, bool aging);
+cudaError_t launch_batch_construct_rows(const ColonyDev *descs, const int4 *items, int num_items,
+                                        int *queue_head, int grid, int ants, int max_n,
+                                        int max_ldk, bool aging, cudaStream_t s);
+cudaError_t launch_nn_to_i16(const int32_t *nn, int n, int K, int ldk, int16_t *nn16,
+                             cudaStream_t s);
 cudaError_t launch_epilogue(const ColonyDev &c, cudaStream_t s);
 
 // ---- batches of instances (descs: one ColonyDev per instance, in device memory) ----

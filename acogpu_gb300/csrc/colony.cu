@@ -119,7 +119,7 @@ int check_params(const aco_params *p, int n) {
   if (p->nn_order == ACO_NN_STABLE && n > 16384) return ACO_ERR_UNSUPPORTED;
   if (p->variant == ACO_RANK_BASED && p->rank_w < 1) return ACO_ERR_INVALID_ARGUMENT;
   if (p->ants_per_block < 0 || p->ants_per_block > 16) return ACO_ERR_INVALID_ARGUMENT;
-  if (p->construct_mode < ACO_CONSTRUCT_AUTO || p->construct_mode > ACO_CONSTRUCT_CLUSTER)
+  if (p->construct_mode < ACO_CONSTRUCT_AUTO || p->construct_mode > ACO_CONSTRUCT_ROWS)
     return ACO_ERR_INVALID_ARGUMENT;
   if (p->fallback_tier < ACO_FALLBACK_TIER_AUTO || p->fallback_tier > ACO_FALLBACK_TIER_OFF)
     return ACO_ERR_INVALID_ARGUMENT;
@@ -127,6 +127,8 @@ int check_params(const aco_params *p, int n) {
     return ACO_ERR_UNSUPPORTED;
   if ((p->construct_mode == ACO_CONSTRUCT_DIRECT || p->construct_mode == ACO_CONSTRUCT_CLUSTER) &&
       (K > 32 || n > kDirectMaxCities))
+    return ACO_ERR_UNSUPPORTED;
+  if (p->construct_mode == ACO_CONSTRUCT_ROWS && (K <= 32 || n > kRowsMaxCities))
     return ACO_ERR_UNSUPPORTED;
   return ACO_OK;
 }
@@ -152,8 +154,11 @@ int allocate(aco_colony *c) {
   if ((s = dalloc(c, &c->perf, m))) return s;
   if ((s = dalloc(c, &c->valid, m))) return s;
   if ((s = dalloc(c, &c->mean, ld))) return s;
-  // 16 bytes of slack: the cluster kernel stages slices in 16-byte units
-  if (c->K <= 32 && c->n < 32768 && (s = dalloc(c, &c->nn16, n * ldk + 8))) return s;
+  // Candidate ids as int16, for the k <= 32 kernels and the long-row kernel
+  // (16 bytes of slack: the cluster kernel stages slices in 16-byte units).
+  if ((c->K <= 32 ? c->n < 32768 : c->n <= kRowsMaxCities) &&
+      (s = dalloc(c, &c->nn16, n * ldk + 8)))
+    return s;
   // The fallback's second tier, for the k <= 32 step loop.
   const bool tier = c->p.fallback_tier == ACO_FALLBACK_TIER_ON ||
                     (c->p.fallback_tier == ACO_FALLBACK_TIER_AUTO &&
@@ -247,7 +252,9 @@ int read_state(aco_colony *c, ColonyState *h) {
 
 // Launches of one construction: the staged kernel of an aging colony is
 // preceded by the plan of the ants' roles.
-int construction_launches(const aco_colony *c) { return c->staged && c->p.aging ? 2 : 1; }
+int construction_launches(const aco_colony *c) {
+  return (c->staged || c->rows) && c->p.aging ? 2 : 1;
+}
 
 cudaError_t launch_construction(aco_colony *c, const ColonyDev &d) {
   if (c->staged) {
@@ -257,6 +264,7 @@ cudaError_t launch_construction(aco_colony *c, const ColonyDev &d) {
     }
     return launch_construct_staged(d, c->nn16, c->staged_grid, c->staged_warps, c->stream);
   }
+  if (c->rows) return launch_construct_rows(d, c->staged_grid, c->staged_warps, c->stream);
   if (c->cluster)
     return launch_construct_cluster(d, c->staged_grid, c->staged_warps, c->cluster, c->stream);
   if (c->direct) return launch_construct_direct(d, c->staged_grid, c->staged_warps, c->stream);
@@ -268,14 +276,32 @@ cudaError_t launch_construction(aco_colony *c, const ColonyDev &d) {
 // the cluster kernel (the table split over ceil(n/1024) CTAs, n <= 8192),
 // else the direct kernel (the same step loop on rows read from L2); otherwise,
 // and in ACO_CONSTRUCT_GLOBAL mode, the general global-memory kernel.  The
-// k <= 32 kernels put one ant per warp.
+// k <= 32 kernels put one ant per warp.  For k > 32 (mode AUTO or ROWS) the
+// long-row kernel: A ants a CTA (a scan warp each, plus the chain warp), one
+// CTA per SM, the ants spread evenly over the SMs (each ant's steps are a
+// latency-bound chain of float adds).
 int plan_construction(aco_colony *c) {
   c->staged = false;
   c->direct = false;
   c->cluster = 0;
+  c->rows = false;
   const int mode = c->p.construct_mode;
-  if (c->K > 32 || !c->nn16 || mode == ACO_CONSTRUCT_GLOBAL) return ACO_OK;
   const int sms = c->num_sms > 0 ? c->num_sms : 1;
+  if (c->nn16 && c->n <= kRowsMaxCities && c->K > 32 &&
+      (mode == ACO_CONSTRUCT_ROWS || mode == ACO_CONSTRUCT_AUTO)) {
+    const size_t per_ant = rows_ant_bytes(c->n, c->K, c->ldk);
+    const size_t avail = (size_t)c->max_smem_optin - 1024;  // static shared memory
+    int ants = (c->m + sms - 1) / sms;
+    ants = std::max(1, std::min(ants, kRowsMaxAnts));
+    ants = std::min<int>(ants, (int)(avail / per_ant));
+    if (ants < 1) return fail(c, ACO_ERR_UNSUPPORTED, "a long row does not fit in shared memory");
+    ACO_CUDA(c, configure_construct_rows((size_t)ants * per_ant), "configure row construct");
+    c->rows = true;
+    c->staged_warps = ants;
+    c->staged_grid = std::min(sms, (c->m + ants - 1) / ants);
+    return ACO_OK;
+  }
+  if (c->K > 32 || !c->nn16 || mode == ACO_CONSTRUCT_GLOBAL) return ACO_OK;
   int warps = (c->m + sms - 1) / sms;
   warps = warps < 1 ? 1 : (warps > kStagedMaxWarps ? kStagedMaxWarps : warps);
   int grid = (c->m + warps - 1) / warps;
@@ -526,7 +552,7 @@ int aco_colony_initialize(aco_colony *c) {
   }
   ACO_CUDA(c, launch_gather_nn_f32(c->eta, n, c->ld, c->nn, c->K, c->ldk, c->eta_nn, c->stream),
            "eta_nn");
-  if (c->nn16) ACO_CUDA(c, launch_nn_to_i16(c->nn, n, c->ldk, c->nn16, c->stream), "nn16");
+  if (c->nn16) ACO_CUDA(c, launch_nn_to_i16(c->nn, n, c->K, c->ldk, c->nn16, c->stream), "nn16");
 
   const ColonyDev d = make_dev(c);
   ACO_CUDA(c, launch_greedy_tau0(d, c->p.tau0_mode, c->p.tau0, c->stream), "tau0");
@@ -894,6 +920,8 @@ struct aco_batch {
   int apb = 8, row_threads = 256, grid = 0;
   size_t region_bytes = 0;  // shared region of the construction launch
   int staged_count = 0;     // instances built from a staged table
+  bool rows = false;        // construction by the long-row batch kernel (every k > 32)
+  int min_k = 1 << 30, max_ldk_rows = 0;
   bool initialized = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -964,7 +992,13 @@ int batch_build_items(aco_batch *b) {
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int c) { return b->cols[a]->n > b->cols[c]->n; });
   std::vector<char> staged;
-  b->region_bytes = batch_plan_region(b, b->apb, &staged, &b->staged_count);
+  if (b->rows) {
+    staged.assign(b->cols.size(), 0);
+    b->region_bytes = 0;
+    b->staged_count = 0;
+  } else {
+    b->region_bytes = batch_plan_region(b, b->apb, &staged, &b->staged_count);
+  }
   std::vector<int4> items;
   for (int i : order) {
     const int m = b->cols[i]->m;
@@ -977,6 +1011,15 @@ int batch_build_items(aco_batch *b) {
   ACO_BCUDA(b, upload_sync(b, b->d_items, items.data(), items.size() * sizeof(int4)),
             "upload items");
   b->num_items = (int)items.size();
+  if (b->rows) {
+    const size_t smem = batch_rows_smem_bytes(b->max_n, b->max_ldk_rows, b->apb);
+    if (b->apb > kRowsMaxAnts || smem + 1024 > (size_t)b->max_smem_optin)
+      return bfail(b, ACO_ERR_UNSUPPORTED, "too many ants per CTA for the long rows' buffers");
+    ACO_BCUDA(b, configure_batch_construct_rows(smem), "configure batch row construct");
+    b->grid = b->num_sms * batch_rows_blocks_per_sm(b->apb, smem, b->p.aging != 0);
+    batch_drop_graph(b);
+    return ACO_OK;
+  }
   const size_t smem = batch_construct_smem_bytes(b->region_bytes, b->apb);
   ACO_BCUDA(b, configure_batch_construct(smem), "configure batch construct");
   b->grid = b->num_sms * batch_construct_blocks_per_sm(b->apb, smem, b->max_k > 32, b->sp,
@@ -989,10 +1032,21 @@ int batch_enqueue(aco_batch *b, bool construct, bool epilogue, bool rows, bool u
   for (aco_colony *c : b->cols) state_changed(c);
   if (construct) {
     ACO_BCUDA(b, cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream), "reset queue");
-    ACO_BCUDA(b, launch_batch_construct(b->d_descs, b->d_items, b->num_items, b->d_queue, b->grid,
-                                        b->apb, b->max_n, b->max_k, b->region_bytes, b->sp,
-                                        b->p.aging != 0, b->stream),
-              "batch construct");
+    if (b->rows && b->p.aging) {
+      ACO_BCUDA(b, launch_batch_aging_plan(b->d_descs, (int)b->cols.size(), b->stream),
+                "batch aging plan");
+      b->launches++;
+    }
+    if (b->rows)
+      ACO_BCUDA(b, launch_batch_construct_rows(b->d_descs, b->d_items, b->num_items, b->d_queue,
+                                               b->grid, b->apb, b->max_n, b->max_ldk_rows,
+                                               b->p.aging != 0, b->stream),
+                "batch row construct");
+    else
+      ACO_BCUDA(b, launch_batch_construct(b->d_descs, b->d_items, b->num_items, b->d_queue,
+                                          b->grid, b->apb, b->max_n, b->max_k, b->region_bytes,
+                                          b->sp, b->p.aging != 0, b->stream),
+                "batch construct");
     b->launches++;
   }
   if (epilogue) {
@@ -1056,11 +1110,26 @@ int aco_batch_create(const aco_params *params, int32_t count, const int32_t *siz
     off += 2 * (size_t)n;
     b->max_n = std::max(b->max_n, c->n);
     b->max_k = std::max(b->max_k, c->K);
+    b->min_k = std::min(b->min_k, c->K);
+    b->max_ldk_rows = std::max(b->max_ldk_rows, c->ldk);
     if (c->K <= 32) b->sp = std::max(b->sp, c->ldk);
     b->max_ld = std::max(b->max_ld, c->ld);
     b->total_rows += n;
   }
   if (b->sp == 0) b->sp = 32;
+  // Candidate rows longer than 32 in every instance (full rows included):
+  // the long-row batch kernel, when every instance has int16 ids and one
+  // ant's buffers fit.
+  b->rows = b->min_k > 32 && params->construct_mode != ACO_CONSTRUCT_GLOBAL &&
+            batch_rows_smem_bytes(b->max_n, b->max_ldk_rows, 1) + 1024 <=
+                (size_t)b->max_smem_optin;
+  for (aco_colony *c : b->cols)
+    if (!c->nn16) b->rows = false;
+  if (b->rows) b->apb = std::min(b->apb, kRowsMaxAnts);
+  while (b->rows && b->apb > 1 &&
+         batch_rows_smem_bytes(b->max_n, b->max_ldk_rows, b->apb) + 1024 >
+             (size_t)b->max_smem_optin)
+    b->apb--;
   *out = b;
   return ACO_OK;
 }
@@ -1116,7 +1185,7 @@ int aco_batch_run(aco_batch *b, int32_t iterations) {
   }
   for (int32_t i = 0; i < iterations; i++)
     ACO_BCUDA(b, cudaGraphLaunch(b->graph_exec, b->stream), "graph launch");
-  b->launches += 3 * (int64_t)iterations;
+  b->launches += (3 + (b->rows && b->p.aging ? 1 : 0)) * (int64_t)iterations;
   return ACO_OK;
 }
 
@@ -1131,13 +1200,19 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int apbs[5] = {1, 2, 4, 8, 16};  // the kernel is launch-bounded to 512 threads
+  // Ants per CTA: warps of the k <= 32 kernels (launch-bounded to 512
+  // threads); ants (scan warps, plus the chain warp) of the long-row kernel.
+  const int apbs_short[5] = {1, 2, 4, 8, 16};
+  const int apbs_rows[5] = {2, 4, 6, 8, 11};
+  const int *apbs = b->rows ? apbs_rows : apbs_short;
   float best_ms = 1e30f;
   int best_apb = b->apb;
-  for (int apb : apbs) {
-    if (batch_construct_smem_bytes(batch_plan_region(b, apb, nullptr, nullptr), apb) >
-        (size_t)b->max_smem_optin)
-      continue;
+  for (int ai = 0; ai < 5; ai++) {
+    const int apb = apbs[ai];
+    const size_t need = b->rows ? batch_rows_smem_bytes(b->max_n, b->max_ldk_rows, apb) + 1024
+                                : batch_construct_smem_bytes(
+                                      batch_plan_region(b, apb, nullptr, nullptr), apb);
+    if (need > (size_t)b->max_smem_optin || (b->rows && apb > kRowsMaxAnts)) continue;
     b->apb = apb;
     if (int s = batch_build_items(b)) return s;
     float ms = 1e30f;

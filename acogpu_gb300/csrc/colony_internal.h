@@ -36,6 +36,7 @@ struct aco_colony {
   bool staged = false;      // construction by the staged kernel
   bool direct = false;      // construction by the direct (L2-row) kernel
   int cluster = 0;          // construction by the cluster kernel: CTAs per cluster
+  bool rows = false;        // construction by the long-row kernel (k > 32)
   int32_t *nn2 = nullptr;   // fallback second tier (see ColonyDev)
   float *t2v = nullptr;
   float *mout = nullptr;

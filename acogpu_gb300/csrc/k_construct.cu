@@ -56,7 +56,7 @@ __device__ __forceinline__ int2 block_exclusive_scan2(int2 v, int2 *s_warp, int2
   return make_int2(before.x + x.x - v.x, before.y + x.y - v.y);
 }
 
-__global__ void __launch_bounds__(1024) k_aging_plan(ColonyDev c) {
+__device__ __forceinline__ void aging_plan_body(const ColonyDev &c) {
   __shared__ int2 s_warp[32];
   __shared__ int2 s_total;
   const int tid = threadIdx.x, T = blockDim.x;
@@ -93,8 +93,20 @@ __global__ void __launch_bounds__(1024) k_aging_plan(ColonyDev c) {
   }
 }
 
+__global__ void __launch_bounds__(1024) k_aging_plan(ColonyDev c) { aging_plan_body(c); }
+
+// One CTA per instance of a batch.
+__global__ void __launch_bounds__(1024) k_batch_aging_plan(const ColonyDev *__restrict__ descs) {
+  aging_plan_body(descs[blockIdx.x]);
+}
+
 cudaError_t launch_aging_plan(const ColonyDev &c, cudaStream_t s) {
   k_aging_plan<<<1, 1024, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_aging_plan(const ColonyDev *descs, int count, cudaStream_t s) {
+  k_batch_aging_plan<<<count, 1024, 0, s>>>(descs);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,846 @@
+// k_construct_rows.cu -- tour construction over long candidate rows (k > 32,
+// the reference's full-row roulette included).
+//
+// Replaces the reference CPU step calculateProbabilityOfSelection +
+// selectCities / chooseBestNext (src/Colony.cu:795-864) and the GPU kernels
+// dev_compute_probabilities / dev_reduce_probabilities_s / dev_move_ants
+// (inc/Colony.cuh:193-229,290-347; src/Colony.cu:643-685).  The reference
+// walks all n entries of the current city's nn row for every ant and step:
+// it adds the weight of every unvisited entry, in row order, into sum_prob,
+// then walks the same entries again until the running sum exceeds
+// u * sum_prob.  Visited entries carry weight 0, and adding +0 leaves a
+// non-negative float sum unchanged, so the same bits come out of a walk over
+// the non-zero weights alone, in row order.
+//
+// The sequential float sum is the step's critical path: one dependent add
+// per unvisited city of the row, about n^2/2 adds per tour, which no
+// reordering may shorten without changing the rounding.  The kernel is built
+// around it.  A CTA holds A ants (A <= kRowsMaxAnts) of one instance, all at
+// the same step, and A + 1 warps:
+//
+//  * scan warp a (one per ant): one lane copies the row it needs (choice
+//    values, or tau and eta for an ant that blends its fitness, and the int16
+//    city ids) into the ant's staging area with TMA bulk copies on an
+//    mbarrier; the warp then zeroes the weights of visited cities (a bit per
+//    city in shared memory) and compacts the non-zero weights, in row order,
+//    into one of the ant's two buffers (a lane's offset is the count of the
+//    lanes before it, from three ballots of the count bits);
+//  * the chain warp: lane a adds ant a's compacted weights in order,
+//    s = fl(s + w) (sum_prob += prob_ptr[i], partial_sum += prob_ptr[i],
+//    src/Colony.cu:814,840), writes every running sum over its weight, and
+//    records the sum at the end of every 32 entries and the total S.  The A
+//    chains share one instruction stream.
+//
+// One step: the scan warps hand their buffers to the chain warp (named
+// barrier R).  While the chain runs, each scan warp compacts the row of its
+// guessed pick -- staged by TMA as soon as the guess was made -- into its
+// other buffer, and from that row's weights, still in registers, guesses the
+// pick after it (an approximate prefix: chunk sums, a scan over chunks and
+// lanes, the same crossing rule) and starts the copy of that city's row.
+// When the chain is done (named barrier C) the scan warp finds the exact
+// pick: rnd = fl(u * S) (src/Colony.cu:826-828); the first 32-entry block
+// whose recorded end sum exceeds rnd, then in that block the first running
+// sum with !(sum <= rnd) -- written sum > rnd || rnd is NaN, as in the
+// k <= 32 step loop -- is the pick (sums never decrease).  No crossing
+// (S <= 0, u * S rounding to S, or S = +inf from an infinite weight) takes
+// the fallback, as the reference does (chooseBestNext / select_local_best).
+// A right guess (nearly always: the approximate and the exact prefix differ
+// by a few ulps) leaves the next row compacted before the chain ends, so row
+// loads and scans stay off the critical path; a wrong one is undone and the
+// row of the real pick is fetched and scanned.
+//
+// Every warp of a CTA passes the two named barriers once per step, n - 1
+// steps per item, with no early exit: an inconsistency is recorded in the
+// colony's error word and the step continues on a stand-in city.  Every
+// mbarrier wait is bounded (kMaxPolls) and records a timeout, and no staging
+// copy is left in flight at the end of an item.
+#include "k_construct_steps.cuh"
+
+namespace aco {
+
+// ---- shared-memory layout -------------------------------------------------
+
+// Per-ant region (rows_ant_bytes, a multiple of 128 plus 16 so the regions of
+// consecutive ants start four banks apart and the chain warp's 16-byte reads
+// of A buffers at once spread over the banks; offsets in rows_layout).
+// S = rows_slots(K), P = ldk:
+//   w[2]:  2 x S f32        compacted weights (two buffers); the chain warp
+//                           overwrites each weight with the running sum
+//   id[2]: 2 x S int32      their city ids
+//   bend:  S/32 f32         running sum at the end of every 32 entries
+//   sw:    P f32            staged row: choice values (or tau)
+//   se:    P f32            staged row: eta (aging blend)
+//   si:    P int16          staged row: city ids
+//   tw:    tabu bits        visited cities, 32 a word (words padded to 4)
+// The staging mbarriers sit in static shared memory (their place must not
+// depend on an instance's layout).  Buffer b is addressed arithmetically (no
+// array of pointers, which a run-time index would move to local memory).
+struct RowsAnt {
+  float *w0;
+  int32_t *id0;
+  float *bend;
+  float *sw;
+  float *se;
+  int16_t *si;
+  uint32_t *tw;
+  uint64_t *bar;
+  int S;
+  __device__ __forceinline__ float *w(int b) const { return w0 + b * S; }
+  __device__ __forceinline__ int32_t *id(int b) const { return id0 + b * S; }
+};
+
+__device__ __forceinline__ RowsAnt rows_ant_at(unsigned char *base, int n, int K, int P,
+                                               uint64_t *bar) {
+  const RowsLayout L = rows_layout(n, K, P);
+  RowsAnt r;
+  r.S = L.S;
+  r.w0 = reinterpret_cast<float *>(base);
+  r.id0 = reinterpret_cast<int32_t *>(base + L.id_off);
+  r.bend = reinterpret_cast<float *>(base + L.bend_off);
+  r.sw = reinterpret_cast<float *>(base + L.sw_off);
+  r.se = reinterpret_cast<float *>(base + L.se_off);
+  r.si = reinterpret_cast<int16_t *>(base + L.si_off);
+  r.tw = reinterpret_cast<uint32_t *>(base + L.tw_off);
+  r.bar = bar;
+  return r;
+}
+
+// Chain length of step x: the entries a compacted buffer can hold at that
+// step (at most min(K, n - x) non-zero weights), rounded up to whole blocks
+// of 32; every buffer is zero-padded to it.
+__device__ __forceinline__ int rows_chain_len(int K, int n, int x) {
+  const int c = K < n - x ? K : n - x;
+  return (c + 31) & ~31;
+}
+
+__device__ __forceinline__ void named_bar_sync(int id, int threads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+__device__ __forceinline__ void named_bar_arrive(int id, int threads) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+constexpr int kBarRowsReady = 1, kBarChainDone = 2;
+
+// ---- scan warp: staging ----------------------------------------------------
+
+// Starts the copy of the row of `city` into the staging area (lane 0; the
+// warp's earlier reads of the area are complete).  Row starts are 128-byte
+// aligned (ldk % 32 == 0) and the sizes multiples of 64 bytes.
+__device__ __forceinline__ void rows_stage(const ColonyDev &c, const RowsAnt &ra, int city,
+                                           bool blend, int lane) {
+  __syncwarp();
+  if (lane == 0) {
+    fence_proxy_async();  // the area's earlier generic-proxy reads come first
+    const size_t off = (size_t)city * c.ldk;
+    const uint32_t wb = (uint32_t)c.ldk * 4u, ib = (uint32_t)c.ldk * 2u;
+    mbar_arrive_expect_tx(ra.bar, (blend ? 2u * wb : wb) + ib);
+    if (!blend) {
+      tma_load_1d(ra.sw, c.choice_nn + off, wb, ra.bar);
+    } else {
+      tma_load_1d(ra.sw, c.tau_nn + off, wb, ra.bar);
+      tma_load_1d(ra.se, c.eta_nn + off, wb, ra.bar);
+    }
+    tma_load_1d(ra.si, c.nn16 + off, ib, ra.bar);
+  }
+}
+
+// Waits (bounded) for the staging copies of the current phase.
+__device__ __forceinline__ void rows_stage_wait(const ColonyDev &c, const RowsAnt &ra,
+                                                uint32_t &phase) {
+  mbar_wait_bounded(ra.bar, phase, c.st);
+  phase ^= 1u;
+}
+
+// ---- scan warp: compaction -------------------------------------------------
+
+// Visited masking of one chunk (four consecutive row positions p0 .. p0+3 of
+// this lane): the weights (bits) of visited cities and of positions past K
+// become 0; bit t of the result is set where entry t stays non-zero.  Ids
+// past K (-1 in the table) are replaced by city 0 so the lookup stays in the
+// list.
+template <bool PARTIAL>
+__device__ __forceinline__ unsigned rows_mask4(uint4 &wbits, uint2 &ip, int p0, int K,
+                                               const uint32_t *tw) {
+  int id[4] = {(int)(ip.x & 0xffffu), (int)(ip.x >> 16), (int)(ip.y & 0xffffu),
+               (int)(ip.y >> 16)};
+  uint32_t wb[4] = {wbits.x, wbits.y, wbits.z, wbits.w};
+  unsigned nz = 0u;
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    if (PARTIAL && p0 + t >= K) id[t] = 0;
+    const bool seen = (tw[id[t] >> 5] >> (id[t] & 31)) & 1u;
+    if (seen || (PARTIAL && p0 + t >= K)) wb[t] = 0u;
+    nz |= ((wb[t] << 1) != 0u ? 1u : 0u) << t;  // non-zero (weights are never -0)
+  }
+  wbits = make_uint4(wb[0], wb[1], wb[2], wb[3]);
+  if (PARTIAL)
+    ip = make_uint2((uint32_t)id[0] | ((uint32_t)id[1] << 16),
+                    (uint32_t)id[2] | ((uint32_t)id[3] << 16));
+  return nz;
+}
+
+// Approximate pick of a row still in registers (one round of JB = 8 chunks
+// of 128 entries): the chunk sums (a transposing butterfly: each of three
+// levels hands half of a lane's chunk sums to its partner, so lane l ends
+// with a partial sum of chunk l >> 2, then two plain levels), their scan over
+// chunks, the first chunk where the running total passes u * S', then within
+// it the lanes' inclusive scan and the entry of the first lane that passes.
+// Any summation order will do: the guess only decides which row is staged
+// early.  Returns the city, or -1.
+template <int JB>
+__device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2 (&ip)[JB],
+                                               float u, int lane) {
+  static_assert(JB == 8, "the transposing butterfly assumes eight chunks");
+  float ls[JB];
+#pragma unroll
+  for (int j = 0; j < JB; j++)
+    ls[j] = (__uint_as_float(q[j].x) + __uint_as_float(q[j].y)) +
+            (__uint_as_float(q[j].z) + __uint_as_float(q[j].w));
+  const bool h4 = (lane >> 4) & 1, h3 = (lane >> 3) & 1, h2 = (lane >> 2) & 1;
+  float t4[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float keep = h4 ? ls[i + 4] : ls[i], give = h4 ? ls[i] : ls[i + 4];
+    t4[i] = keep + __shfl_xor_sync(kFull, give, 16);
+  }
+  float t2[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    const float keep = h3 ? t4[i + 2] : t4[i], give = h3 ? t4[i] : t4[i + 2];
+    t2[i] = keep + __shfl_xor_sync(kFull, give, 8);
+  }
+  float t1;
+  {
+    const float keep = h2 ? t2[1] : t2[0], give = h2 ? t2[0] : t2[1];
+    t1 = keep + __shfl_xor_sync(kFull, give, 4);
+  }
+  t1 += __shfl_xor_sync(kFull, t1, 2);
+  t1 += __shfl_xor_sync(kFull, t1, 1);  // lane l: the sum of chunk l >> 2
+  float inc = t1;                       // inclusive scan over chunks (lanes 0, 4, .., 28)
+#pragma unroll
+  for (int o = 4; o < 32; o <<= 1) {
+    const float y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += y;
+  }
+  const float S = __shfl_sync(kFull, inc, 28);
+  if (!(S > 0.0f) || !(S < INFINITY)) return -1;
+  const float rnd = u * S;
+  const unsigned hc = __ballot_sync(kFull, (lane & 3) == 0 && inc > rnd);
+  if (!hc) return -1;
+  const int l0 = __ffs(hc) - 1;  // 4 * chunk
+  const int js = l0 >> 2;
+  const float base = __shfl_sync(kFull, inc - t1, l0);
+  float x = ls[0];
+  uint4 qq = q[0];
+  uint2 ii = ip[0];
+#pragma unroll
+  for (int j = 1; j < JB; j++) {
+    if (js == j) {
+      x = ls[j];
+      qq = q[j];
+      ii = ip[j];
+    }
+  }
+  float incl = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const float y = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += y;
+  }
+  incl += base;
+  const unsigned hit = __ballot_sync(kFull, incl > rnd);
+  if (!hit) return -1;
+  const int l = __ffs(hit) - 1;
+  const float w[4] = {__uint_as_float(qq.x), __uint_as_float(qq.y), __uint_as_float(qq.z),
+                      __uint_as_float(qq.w)};
+  const int id[4] = {(int)(ii.x & 0xffffu), (int)(ii.x >> 16), (int)(ii.y & 0xffffu),
+                     (int)(ii.y >> 16)};
+  float acc = incl - x;
+  int city = -1;
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    acc += w[t];
+    if (city < 0 && w[t] != 0.0f && acc > rnd) city = id[t];
+  }
+  return __shfl_sync(kFull, city, l);
+}
+
+// Approximate pick of a compacted buffer (rows of more than 128 JB entries):
+// block sums of 32 entries (each lane one block, its eight 16-byte reads in
+// a lane-rotated order so the lanes spread over the banks), their inclusive
+// warp scan, the first block past u * S', then within it the lanes'
+// masked-FMA prefixes from the block's approximate start.  NR rounds of 32
+// blocks (cnt <= 1024 NR).  Returns the city, or -1.
+template <int NR>
+__device__ __forceinline__ int rows_guess_smem(const float *w, const int32_t *id, int cnt, float u,
+                                               int lane) {
+  if (cnt <= 0 || cnt > 1024 * NR) return -1;
+  const float4 *w4 = reinterpret_cast<const float4 *>(w);
+  float bs[NR];
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    const int b = r * 32 + lane;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    if (b * 32 < cnt) {
+#pragma unroll
+      for (int g = 0; g < 8; g++) {
+        const float4 v = w4[b * 8 + ((g + lane) & 7)];  // zero-padded past cnt
+        s0 += v.x;
+        s1 += v.y;
+        s2 += v.z;
+        s3 += v.w;
+      }
+    }
+    bs[r] = (s0 + s1) + (s2 + s3);
+  }
+  float carry = 0.0f, incl[NR];
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    float x = bs[r];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    incl[r] = carry + x;
+    carry += __shfl_sync(kFull, x, 31);
+  }
+  const float S = carry;
+  if (!(S > 0.0f) || !(S < INFINITY)) return -1;
+  const float rnd = u * S;
+  int blk = -1;
+  float start = 0.0f;
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    const unsigned hit = __ballot_sync(kFull, (r * 32 + lane) * 32 < cnt && incl[r] > rnd);
+    if (hit && blk < 0) {
+      const int l = __ffs(hit) - 1;
+      blk = r * 32 + l;
+      start = __shfl_sync(kFull, incl[r] - bs[r], l);
+    }
+  }
+  if (blk < 0) return -1;
+  float acc = start;
+  const float4 *b4 = w4 + blk * 8;
+#pragma unroll
+  for (int g = 0; g < 8; g++) {
+    const float4 v = b4[g];
+    acc = __fmaf_rn(v.x, 4 * g + 0 <= lane ? 1.0f : 0.0f, acc);
+    acc = __fmaf_rn(v.y, 4 * g + 1 <= lane ? 1.0f : 0.0f, acc);
+    acc = __fmaf_rn(v.z, 4 * g + 2 <= lane ? 1.0f : 0.0f, acc);
+    acc = __fmaf_rn(v.w, 4 * g + 3 <= lane ? 1.0f : 0.0f, acc);
+  }
+  const unsigned hit = __ballot_sync(kFull, blk * 32 + lane < cnt && acc > rnd);
+  if (!hit) return -1;
+  return id[blk * 32 + __ffs(hit) - 1];
+}
+
+struct RowsScan {
+  int cnt;    // non-zero weights written
+  int guess;  // approximate pick (u >= 0), or -1
+};
+
+// Steps of the header for the staged row (the copy is complete): into wo/io,
+// zero-padded to L; with u >= 0 also the approximate pick of that row.  JB
+// chunks of 128 entries per round: all of a round's shared loads first, then
+// every chunk's visited lookups, then the ballots of every chunk, then the
+// compacting stores.
+template <int JB>
+__device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt &ra, bool blend,
+                                              float meanc, float ratio, float *wo, int32_t *io,
+                                              int L, float u, int lane) {
+  const int K = c.K;
+  RowsScan r;
+  r.cnt = 0;
+  r.guess = -1;
+#pragma unroll 1
+  for (int j0 = 0; j0 < K; j0 += JB * 128) {
+    uint4 q[JB];
+    uint2 ip[JB];
+    unsigned nz[JB];
+#pragma unroll
+    for (int j = 0; j < JB; j++) {
+      const int p0 = j0 + j * 128 + lane * 4;
+      const bool in = p0 < K;  // p0 < K <= ldk, ldk % 4 == 0: the four entries are staged
+      ip[j] = in ? *reinterpret_cast<const uint2 *>(ra.si + p0) : make_uint2(0u, 0u);
+      if (!blend) {
+        q[j] = in ? *reinterpret_cast<const uint4 *>(ra.sw + p0) : make_uint4(0, 0, 0, 0);
+      } else {
+        const float4 t = in ? *reinterpret_cast<const float4 *>(ra.sw + p0)
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 e = in ? *reinterpret_cast<const float4 *>(ra.se + p0)
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+        q[j].x = __float_as_uint(blend_fitness(t.x, e.x, meanc, ratio, c.use_alpha, c.alpha));
+        q[j].y = __float_as_uint(blend_fitness(t.y, e.y, meanc, ratio, c.use_alpha, c.alpha));
+        q[j].z = __float_as_uint(blend_fitness(t.z, e.z, meanc, ratio, c.use_alpha, c.alpha));
+        q[j].w = __float_as_uint(blend_fitness(t.w, e.w, meanc, ratio, c.use_alpha, c.alpha));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < JB; j++) {
+      const int c0 = j0 + j * 128;
+      nz[j] = 0u;
+      if (c0 < K) {  // warp-uniform
+        if (c0 + 128 <= K)
+          nz[j] = rows_mask4<false>(q[j], ip[j], c0 + lane * 4, K, ra.tw);
+        else
+          nz[j] = rows_mask4<true>(q[j], ip[j], c0 + lane * 4, K, ra.tw);
+      } else {
+        q[j] = make_uint4(0, 0, 0, 0);
+      }
+    }
+    if (u >= 0.0f && K <= JB * 128) r.guess = rows_guess_regs<JB>(q, ip, u, lane);
+    // A lane's offset in chunk j: the counts of the lanes before it, from
+    // three ballots of the count bits; every chunk's ballots first.
+    const unsigned lt = (1u << lane) - 1u;
+    int off[JB], tot[JB];
+#pragma unroll
+    for (int j = 0; j < JB; j++) {
+      const int cl = __popc(nz[j]);
+      const unsigned b0 = __ballot_sync(kFull, cl & 1), b1 = __ballot_sync(kFull, cl & 2),
+                     b2 = __ballot_sync(kFull, cl & 4);
+      off[j] = __popc(b0 & lt) + 2 * __popc(b1 & lt) + 4 * __popc(b2 & lt);
+      tot[j] = __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
+    }
+#pragma unroll
+    for (int j = 0; j < JB; j++) {
+      int o = r.cnt + off[j];
+      const uint32_t wb[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
+      const int id[4] = {(int)(ip[j].x & 0xffffu), (int)(ip[j].x >> 16),
+                         (int)(ip[j].y & 0xffffu), (int)(ip[j].y >> 16)};
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        if ((nz[j] >> t) & 1u) {
+          wo[o] = __uint_as_float(wb[t]);
+          io[o] = id[t];
+          o++;
+        }
+      }
+      r.cnt += tot[j];
+    }
+  }
+  for (int i = r.cnt + lane; i < L; i += 32) wo[i] = 0.0f;
+  if (u >= 0.0f && K > JB * 128) {
+    __syncwarp();
+    r.guess = rows_guess_smem<2>(wo, io, r.cnt, u, lane);
+  }
+  return r;
+}
+
+// Exact pick (see the header): the first block of 32 whose recorded end sum
+// passes rnd = fl(u * S), then in the running sums pf that the chain warp
+// wrote over that block the first entry with !(pf <= rnd).  Entries past
+// cnt hold S (the padding adds zeros) and are not candidates.  Index, or -1.
+__device__ __forceinline__ int rows_exact(const float *pf, const float *bend, int cnt, int L,
+                                          float S, float u, int lane) {
+  if (S <= 0.0f) return -1;  // chooseBestNext (src/Colony.cu:776-778)
+  const float rnd = __fmul_rn(u, S);
+  const bool nan = rnd != rnd;
+  const int nb = L >> 5;
+  int blk = -1;
+#pragma unroll 1
+  for (int b0 = 0; b0 < nb; b0 += 32) {
+    const int bb = b0 + lane;
+    const float e = bb < nb ? bend[bb] : 0.0f;
+    const unsigned hit = __ballot_sync(kFull, bb < nb && (e > rnd || nan));
+    if (hit) {
+      blk = b0 + __ffs(hit) - 1;
+      break;
+    }
+  }
+  if (blk < 0) return -1;
+  const int i = blk * 32 + lane;
+  const float v = pf[i];
+  const unsigned hit = __ballot_sync(kFull, i < cnt && (v > rnd || nan));
+  return hit ? blk * 32 + __ffs(hit) - 1 : -1;
+}
+
+__device__ __forceinline__ void tw_set(uint32_t *tw, int city, bool on, int lane) {
+  __syncwarp();
+  if (lane == 0) {
+    if (on)
+      tw[city >> 5] |= 1u << (city & 31);
+    else
+      tw[city >> 5] &= ~(1u << (city & 31));
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ bool tw_test(const uint32_t *tw, int city) {
+  return (tw[city >> 5] >> (city & 31)) & 1u;
+}
+
+// ---- chain warp --------------------------------------------------------------
+
+__device__ __forceinline__ void rows_chain_add32(float4 *w4, const float4 (&a)[8], float &s) {
+#pragma unroll
+  for (int g = 0; g < 8; g++) {
+    float4 p;
+    s = __fadd_rn(s, a[g].x);
+    p.x = s;
+    s = __fadd_rn(s, a[g].y);
+    p.y = s;
+    s = __fadd_rn(s, a[g].z);
+    p.z = s;
+    s = __fadd_rn(s, a[g].w);
+    p.w = s;
+    w4[g] = p;
+  }
+}
+
+// Lane a < A: the running sums of ant a's buffer w over L entries (a multiple
+// of 32, zero-padded past its count), each written over its weight, the sum
+// at the end of every 32 entries in bend, the total in *S.  Two blocks of 32
+// per trip, each block's weights read while the previous block is added.
+__device__ __forceinline__ void rows_chain(float *w, float *bend, int L, float *S) {
+  float4 *w4 = reinterpret_cast<float4 *>(w);
+  const int nb = L >> 5;
+  float s = 0.0f;
+  float4 a[8], v[8];
+  if (nb > 0) {
+#pragma unroll
+    for (int g = 0; g < 8; g++) a[g] = w4[g];
+  }
+#pragma unroll 1
+  for (int b = 0; b < nb; b += 2) {
+    const bool two = b + 1 < nb;
+    const int nx = two ? b + 1 : b;
+#pragma unroll
+    for (int g = 0; g < 8; g++) v[g] = w4[nx * 8 + g];
+    rows_chain_add32(w4 + b * 8, a, s);
+    bend[b] = s;
+    if (!two) break;
+    const int nx2 = b + 2 < nb ? b + 2 : b + 1;
+#pragma unroll
+    for (int g = 0; g < 8; g++) a[g] = w4[nx2 * 8 + g];
+    rows_chain_add32(w4 + (b + 1) * 8, v, s);
+    bend[b + 1] = s;
+  }
+  *S = s;
+}
+
+// ---- the kernel ----------------------------------------------------------------
+
+// Per-CTA control block in static shared memory: the chain sums, which scan
+// warps hold a valid ant, and the staging mbarriers.
+struct RowsCtl {
+  float S[kRowsMaxAnts];
+  int active[kRowsMaxAnts];
+  uint64_t bar[kRowsMaxAnts];
+};
+
+// One item: ants `first` .. `first + count - 1` of the colony (positions in
+// the aging plan's list when PLAN: the valid ants come first), all warps of
+// the CTA.  `region` holds the A per-ant regions; `phase` is this scan
+// warp's staging-mbarrier parity, carried across items.
+template <bool AGING, bool PLAN>
+__device__ void rows_item(const ColonyDev &c, int first, int count, unsigned char *region,
+                          size_t ant_bytes, RowsCtl &ctl, uint32_t &phase) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int A = (blockDim.x >> 5) - 1;  // scan warps; warp A is the chain warp
+  const int threads = blockDim.x;
+  const int n = c.n, K = c.K;
+  const uint32_t iter = c.st->iteration;
+
+  if (warp < A) {
+    // ---- scan warp: ant of this warp (if any), its aging state
+    int k = -1;
+    bool valid = false;
+    AntCtx a;
+    a.blend = false;
+    a.ratio = 0.0f;
+    a.meanc = 0.0f;
+    if (warp < count) {
+      const int pos = first + warp;
+      if (PLAN) {
+        k = c.plan[2 + pos];
+        valid = pos < c.plan[0] + c.plan[1];
+      } else {
+        k = pos;
+        valid = true;
+      }
+      if (AGING && !PLAN) {  // updateAntAges (src/Colony.cu:353-364)
+        int age = 0;
+        if (lane == 0) {
+          age = c.age[k] + 1;
+          c.age[k] = age;
+        }
+        age = __shfl_sync(kFull, age, 0);
+        valid = c.valid[k] != 0;
+      }
+      if (AGING && valid) {
+        const int age = c.age[k];
+        a.blend = age < c.min_ret && c.st->isconverged;
+        if (a.blend) a.ratio = __fdiv_rn(__int2float_rn(age), __int2float_rn(c.min_ret));
+      }
+      if (!valid) {  // an invalid ant keeps a cleared tour (src/Colony.cu:507-510)
+        int32_t *trow = c.tours + (size_t)k * c.ld;
+        for (int i = lane; i < n; i += 32) trow[i] = 0;
+      }
+    }
+    if (lane == 0) ctl.active[warp] = valid ? 1 : 0;
+    const RowsAnt ra =
+        rows_ant_at(region + (size_t)warp * ant_bytes, n, K, c.ldk, &ctl.bar[warp]);
+    int32_t *trow = valid ? c.tours + (size_t)k * c.ld : nullptr;
+    uint32_t akey = 0;
+    int cur = 0, start = 0, cnt = 0;
+    int guess = -1;         // predicted pick of the current step (its row is being staged)
+    bool inflight = false;  // a staging copy not yet waited for
+    int64_t fallbacks = 0;
+    bool ok = true;
+    if (valid) {
+      for (int i = lane; i < (n + 31) / 32; i += 32) ra.tw[i] = 0u;
+      akey = aco_ant_key(c.seed, iter, (uint32_t)k);
+      start = __float2int_rz(__fmul_rn(aco_uniform_key(akey, 0u), __int2float_rn(n)));
+      if (start >= n) {  // impossible for u < 1; recorded, clamped
+        ok = false;
+        start = n - 1;
+      }
+      cur = start;
+      tw_set(ra.tw, start, true, lane);
+      if (lane == 0) trow[0] = start;
+      if (AGING && a.blend) a.meanc = c.mean[start];
+      rows_stage(c, ra, start, a.blend, lane);
+      rows_stage_wait(c, ra, phase);
+      const RowsScan r0 = rows_scan<8>(c, ra, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
+                                       rows_chain_len(K, n, 1),
+                                       n > 2 ? aco_uniform_key(akey, 1u) : -1.0f, lane);
+      cnt = r0.cnt;
+      if (r0.guess >= 0 && n > 2) {
+        guess = r0.guess;
+        rows_stage(c, ra, guess, a.blend, lane);
+        inflight = true;
+      }
+    }
+    int b = 0;
+#pragma unroll 1
+    for (int x = 1; x < n; x++) {
+      __syncwarp();
+      named_bar_arrive(kBarRowsReady, threads);
+      RowsScan g;  // the guessed city's row, and the guess after it
+      g.cnt = 0;
+      g.guess = -1;
+      bool staged = false;
+      float u = 0.0f;
+      if (valid) {
+        u = aco_uniform_key(akey, (uint32_t)x);
+        if (guess >= 0) {  // its row was staged (x + 1 < n)
+          tw_set(ra.tw, guess, true, lane);
+          const float gm = (AGING && a.blend) ? c.mean[guess] : 0.0f;
+          rows_stage_wait(c, ra, phase);
+          inflight = false;
+          g = rows_scan<8>(c, ra, a.blend, gm, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
+                           rows_chain_len(K, n, x + 1),
+                           x + 2 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : -1.0f, lane);
+          staged = true;
+          if (g.guess >= 0 && x + 2 < n) {
+            rows_stage(c, ra, g.guess, a.blend, lane);
+            inflight = true;
+          } else {
+            g.guess = -1;
+          }
+        }
+      }
+      __syncwarp();
+      named_bar_sync(kBarChainDone, threads);
+      if (valid) {
+        const int L = rows_chain_len(K, n, x);
+        const int i = rows_exact(ra.w(b), ra.bend, cnt, L, ctl.S[warp], u, lane);
+        int next = i >= 0 ? ra.id(b)[i] : -1;
+        const bool hit = staged && next >= 0 && next == guess;
+        if (staged && !hit) tw_set(ra.tw, guess, false, lane);  // undo the guess
+        if (next < 0) {
+          next = fallback_city(c, cur, ra.tw, a, lane);
+          fallbacks++;
+        }
+        if ((unsigned)next >= (unsigned)n || (!hit && tw_test(ra.tw, next))) {
+          ok = false;  // no unvisited city, or a bad id: cannot happen
+          next = cur;
+        }
+        if (!hit) tw_set(ra.tw, next, true, lane);
+        if (lane == 0) trow[x] = next;
+        if (AGING && a.blend) a.meanc = c.mean[next];
+        if (hit) {
+          cnt = g.cnt;
+          guess = g.guess;
+        } else {
+          if (inflight) {  // the copy of a row no longer needed
+            rows_stage_wait(c, ra, phase);
+            inflight = false;
+          }
+          guess = -1;
+          if (x + 1 < n) {
+            rows_stage(c, ra, next, a.blend, lane);
+            rows_stage_wait(c, ra, phase);
+            const RowsScan r = rows_scan<8>(
+                c, ra, a.blend, a.meanc, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
+                rows_chain_len(K, n, x + 1),
+                x + 2 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : -1.0f, lane);
+            cnt = r.cnt;
+            if (r.guess >= 0 && x + 2 < n) {
+              guess = r.guess;
+              rows_stage(c, ra, guess, a.blend, lane);
+              inflight = true;
+            }
+          }
+        }
+        cur = next;
+      }
+      b ^= 1;
+    }
+    if (inflight) rows_stage_wait(c, ra, phase);  // no copy outlives the item
+    if (valid) {
+      __syncwarp();
+      int64_t len = 0;
+#pragma unroll 8
+      for (int i = lane; i < n; i += 32) {
+        const int a0 = trow[i];
+        const int b0 = trow[i + 1 == n ? 0 : i + 1];
+        if ((unsigned)a0 < (unsigned)n && (unsigned)b0 < (unsigned)n) {
+          len += c.dist[(size_t)a0 * c.ld + b0];
+          c.succT[(size_t)a0 * c.ldm + k] = b0;
+          c.predT[(size_t)b0 * c.ldm + k] = a0;
+        } else {
+          ok = false;
+        }
+      }
+      for (int o = 16; o; o >>= 1) len += __shfl_xor_sync(kFull, len, o);
+      if (!__all_sync(kFull, ok) && lane == 0) atomicOr(&c.st->error, kErrCheck);
+      if (lane == 0) {
+        c.newlen[k] = len;
+        if (fallbacks)
+          atomicAdd(reinterpret_cast<unsigned long long *>(&c.st->fallbacks),
+                    (unsigned long long)fallbacks);
+      }
+    }
+  } else {
+    // ---- chain warp: lane a runs ant a's chain
+    int b = 0;
+#pragma unroll 1
+    for (int x = 1; x < n; x++) {
+      named_bar_sync(kBarRowsReady, threads);
+      if (lane < A && ctl.active[lane]) {
+        const RowsAnt ra =
+            rows_ant_at(region + (size_t)lane * ant_bytes, n, K, c.ldk, &ctl.bar[lane]);
+        rows_chain(ra.w(b), ra.bend, rows_chain_len(K, n, x), &ctl.S[lane]);
+      }
+      __syncwarp();
+      named_bar_arrive(kBarChainDone, threads);
+      b ^= 1;
+    }
+  }
+}
+
+// The staging mbarriers (once per launch).
+__device__ __forceinline__ void rows_init_bars(RowsCtl &ctl) {
+  const int warp = threadIdx.x >> 5, A = (blockDim.x >> 5) - 1;
+  if (warp < A && (threadIdx.x & 31) == 0) {
+    mbar_init(&ctl.bar[warp], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+}
+
+// Single colony: CTA g takes ant groups g, g + grid, ... of A ants (A + 1
+// warps a CTA).  With aging the ants come from the plan's list (k_aging_plan
+// updated the ages), valid ones first.
+template <bool AGING>
+__global__ void __launch_bounds__((kRowsMaxAnts + 1) * 32) k_construct_rows(ColonyDev c) {
+  extern __shared__ __align__(16) unsigned char smem_rows[];
+  __shared__ RowsCtl ctl;
+  const int A = (blockDim.x >> 5) - 1;
+  const size_t ant_bytes = rows_ant_bytes(c.n, c.K, c.ldk);
+  rows_init_bars(ctl);
+  uint32_t phase = 0;
+  for (int first = blockIdx.x * A; first < c.m; first += gridDim.x * A) {
+    rows_item<AGING, AGING>(c, first, min(A, c.m - first), smem_rows, ant_bytes, ctl, phase);
+    __syncthreads();
+  }
+}
+
+cudaError_t configure_construct_rows(size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_construct_rows<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_construct_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+  return e;
+}
+
+cudaError_t launch_construct_rows(const ColonyDev &c, int grid, int ants, cudaStream_t s) {
+  const size_t smem = (size_t)ants * rows_ant_bytes(c.n, c.K, c.ldk);
+  if (c.aging) {
+    cudaError_t e = launch_aging_plan(c, s);
+    if (e != cudaSuccess) return e;
+    k_construct_rows<true><<<grid, (ants + 1) * 32, smem, s>>>(c);
+  } else {
+    k_construct_rows<false><<<grid, (ants + 1) * 32, smem, s>>>(c);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Batches: CTAs take (instance, first plan position, ant count, -) items from
+// the work queue (largest instances first) until it is empty.  The per-ant
+// regions are sized for the batch's largest instance and candidate row.
+template <bool AGING>
+__global__ void __launch_bounds__((kRowsMaxAnts + 1) * 32)
+    k_batch_construct_rows(const ColonyDev *__restrict__ descs, const int4 *__restrict__ items,
+                           int num_items, int *queue_head, int max_n, int max_ldk) {
+  extern __shared__ __align__(16) unsigned char smem_brows[];
+  __shared__ ColonyDev s_desc;
+  __shared__ RowsCtl ctl;
+  __shared__ int s_item;
+  const size_t ant_bytes = rows_ant_bytes(max_n, max_ldk, max_ldk);
+  rows_init_bars(ctl);
+  uint32_t phase = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(queue_head, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= num_items) break;
+    const int4 w = items[it];
+    if (threadIdx.x == 0) s_desc = descs[w.x];
+    __syncthreads();
+    rows_item<AGING, AGING>(s_desc, w.y, w.z, smem_brows, ant_bytes, ctl, phase);
+    __syncthreads();  // s_item, s_desc and the regions are rewritten by the next item
+  }
+}
+
+size_t batch_rows_smem_bytes(int max_n, int max_ldk, int ants) {
+  return (size_t)ants * rows_ant_bytes(max_n, max_ldk, max_ldk);
+}
+
+cudaError_t configure_batch_construct_rows(size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_batch_construct_rows<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_batch_construct_rows<true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return e;
+}
+
+int batch_rows_blocks_per_sm(int ants, size_t smem, bool aging) {
+  int blocks = 0;
+  const void *fn = aging ? (const void *)k_batch_construct_rows<true>
+                         : (const void *)k_batch_construct_rows<false>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, (ants + 1) * 32, smem) !=
+      cudaSuccess)
+    return 1;
+  return blocks > 0 ? blocks : 1;
+}
+
+cudaError_t launch_batch_construct_rows(const ColonyDev *descs, const int4 *items, int num_items,
+                                        int *queue_head, int grid, int ants, int max_n,
+                                        int max_ldk, bool aging, cudaStream_t s) {
+  const size_t smem = batch_rows_smem_bytes(max_n, max_ldk, ants);
+  if (aging)
+    k_batch_construct_rows<true><<<grid, (ants + 1) * 32, smem, s>>>(descs, items, num_items,
+                                                                     queue_head, max_n, max_ldk);
+  else
+    k_batch_construct_rows<false><<<grid, (ants + 1) * 32, smem, s>>>(descs, items, num_items,
+                                                                      queue_head, max_n, max_ldk);
+  return cudaGetLastError();
+}
+
+}  // namespace aco

@@ -308,19 +308,20 @@ cudaError_t launch_gather_nn_f32(const float *src, int n, int ld, const int32_t 
   return cudaGetLastError();
 }
 
-// int16 copy of a candidate table with 32 entries per row (the staged
-// construction kernel keeps it in shared memory).
-// int16 copy of the candidate rows (same pitch; the -1 padding carries over).
-__global__ void k_nn_to_i16(const int32_t *__restrict__ nn, int n, int ldk,
+// int16 copy of the candidate rows (same pitch; entries past the K
+// candidates of a row are -1).  The staged kernel keeps the k <= 32 table in
+// shared memory; the long-row kernel copies one row at a time by TMA.
+__global__ void k_nn_to_i16(const int32_t *__restrict__ nn, int n, int K, int ldk,
                             int16_t *__restrict__ nn16) {
   const int64_t total = (int64_t)n * ldk;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
        t += (int64_t)gridDim.x * blockDim.x)
-    nn16[t] = (int16_t)nn[t];
+    nn16[t] = (int)(t % ldk) < K ? (int16_t)nn[t] : (int16_t)-1;
 }
 
-cudaError_t launch_nn_to_i16(const int32_t *nn, int n, int ldk, int16_t *nn16, cudaStream_t s) {
-  k_nn_to_i16<<<304, 256, 0, s>>>(nn, n, ldk, nn16);
+cudaError_t launch_nn_to_i16(const int32_t *nn, int n, int K, int ldk, int16_t *nn16,
+                             cudaStream_t s) {
+  k_nn_to_i16<<<304, 256, 0, s>>>(nn, n, K, ldk, nn16);
   return cudaGetLastError();
 }
 

@@ -116,12 +116,16 @@ enum aco_construct_mode {
   ACO_CONSTRUCT_AUTO = 0,    /* k <= 32: staged when the candidate table fits in one CTA's
                                 shared memory, else split over a thread-block cluster
                                 (n <= 8192), else the step loop on rows read from L2;
-                                otherwise the general kernel */
+                                k > 32 (full rows included): the long-row kernel
+                                (n <= 8192), otherwise the general kernel */
   ACO_CONSTRUCT_GLOBAL = 1,  /* the general kernel: candidate rows read from global memory */
   ACO_CONSTRUCT_STAGED = 2,  /* whole candidate table in shared memory; k <= 32, n <= 2048 */
   ACO_CONSTRUCT_DIRECT = 3,  /* the staged step loop on rows read from L2; k <= 32, n <= 8192 */
-  ACO_CONSTRUCT_CLUSTER = 4  /* the table split over a cluster of ceil(n/1024) CTAs, rows
+  ACO_CONSTRUCT_CLUSTER = 4, /* the table split over a cluster of ceil(n/1024) CTAs, rows
                                 read through distributed shared memory; k <= 32, n <= 8192 */
+  ACO_CONSTRUCT_ROWS = 5     /* the long-row kernel: rows staged by TMA and compacted by a
+                                warp per ant, the roulette's sequential prefix over the
+                                non-zero weights by a chain warp; k > 32, n <= 8192 */
 };
 
 /* Stage timers filled by aco_colony_construct_solution, indexed like the

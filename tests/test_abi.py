@@ -65,7 +65,8 @@ def test_enum_constants_match_the_python_mirror():
     mirrored = {k: v for k, v in consts.items() if hasattr(_abi, k)}
     wrong = {k: (v, getattr(_abi, k)) for k, v in mirrored.items() if getattr(_abi, k) != v}
     assert not wrong, wrong
-    for k in ("ACO_CONSTRUCT_DIRECT", "ACO_CONSTRUCT_CLUSTER", "ACO_FALLBACK_TIER_AUTO",
+    for k in ("ACO_CONSTRUCT_DIRECT", "ACO_CONSTRUCT_CLUSTER", "ACO_CONSTRUCT_ROWS",
+              "ACO_FALLBACK_TIER_AUTO",
               "ACO_FALLBACK_TIER_ON", "ACO_FALLBACK_TIER_OFF", "ACO_ERR_DEVICE_TIMEOUT"):
         assert k in mirrored, k
 
@@ -83,7 +84,7 @@ def test_mode_values_are_checked_before_any_device_call():
     h = ctypes.c_void_p()
     d = np.zeros((40, 40), np.int32)
     ptr = d.ctypes.data_as(ctypes.c_void_p)
-    for field, bad in (("construct_mode", 5), ("construct_mode", -1), ("fallback_tier", 3)):
+    for field, bad in (("construct_mode", 6), ("construct_mode", -1), ("fallback_tier", 3)):
         p = _abi.default_params(cand_k=20, fallback=_abi.ACO_FALLBACK_BEST)
         setattr(p, field, bad)
         assert L.aco_colony_create(ctypes.byref(p), ptr, 40, 0, ctypes.byref(h)) == \
@@ -93,3 +94,12 @@ def test_mode_values_are_checked_before_any_device_call():
         p = _abi.default_params(cand_k=0, construct_mode=mode)
         assert L.aco_colony_create(ctypes.byref(p), ptr, 40, 0, ctypes.byref(h)) == \
             _abi.ACO_ERR_UNSUPPORTED, mode
+    # the long-row kernel: candidate lists longer than 32, n <= 8192
+    p = _abi.default_params(cand_k=20, fallback=_abi.ACO_FALLBACK_BEST,
+                            construct_mode=_abi.ACO_CONSTRUCT_ROWS)
+    assert L.aco_colony_create(ctypes.byref(p), ptr, 40, 0, ctypes.byref(h)) == \
+        _abi.ACO_ERR_UNSUPPORTED
+    p = _abi.default_params(cand_k=0, construct_mode=_abi.ACO_CONSTRUCT_ROWS)
+    big = np.zeros((1, 1), np.int32)
+    assert L.aco_colony_create(ctypes.byref(p), big.ctypes.data_as(ctypes.c_void_p), 8193, 0,
+                               ctypes.byref(h)) == _abi.ACO_ERR_UNSUPPORTED
