@@ -71,10 +71,20 @@ namespace aco {
 //   sw:    P f32            staged row: choice values (or tau)
 //   se:    P f32            staged row: eta (aging blend)
 //   si:    P int16          staged row: city ids
-//   tw:    tabu bits        visited cities, 32 a word (words padded to 4)
+//   tw:    tabu bits        visited cities, 32 a word (words padded to 4; the
+//                           fallback's scans read them)
+//   tb:    tabu bytes       visited cities, 0xff or 0 (the scan's lookups: a
+//                           sign-extended byte is the AND mask itself)
 // The staging mbarriers sit in static shared memory (their place must not
 // depend on an instance's layout).  Buffer b is addressed arithmetically (no
 // array of pointers, which a run-time index would move to local memory).
+//
+// Entry i of a compacted buffer (weights, sums and ids alike) sits in slot
+// i / 4 at component (i % 4) ^ ((i / 32) % 4) (rows_swz).  A chunk's stores
+// put lane l's entries near entry 4l, so lanes l, l + 8, l + 16, l + 24 would
+// hit one bank; the key, which differs between them, spreads them over four.
+// Within a block of 32 entries the key is constant, so a reader of whole
+// blocks undoes it with a fixed permutation.
 struct RowsAnt {
   float *w0;
   int32_t *id0;
@@ -83,6 +93,7 @@ struct RowsAnt {
   float *se;
   int16_t *si;
   uint32_t *tw;
+  uint8_t *tb;
   uint64_t *bar;
   int S;
   __device__ __forceinline__ float *w(int b) const { return w0 + b * S; }
@@ -101,9 +112,12 @@ __device__ __forceinline__ RowsAnt rows_ant_at(unsigned char *base, int n, int K
   r.se = reinterpret_cast<float *>(base + L.se_off);
   r.si = reinterpret_cast<int16_t *>(base + L.si_off);
   r.tw = reinterpret_cast<uint32_t *>(base + L.tw_off);
+  r.tb = base + L.tb_off;
   r.bar = bar;
   return r;
 }
+
+__device__ __forceinline__ int rows_swz(int i) { return i ^ ((i >> 5) & 3); }
 
 // Chain length of step x: the entries a compacted buffer can hold at that
 // step (at most min(K, n - x) non-zero weights), rounded up to whole blocks
@@ -154,29 +168,29 @@ __device__ __forceinline__ void rows_stage_wait(const ColonyDev &c, const RowsAn
 // ---- scan warp: compaction -------------------------------------------------
 
 // Visited masking of one chunk (four consecutive row positions p0 .. p0+3 of
-// this lane): the weights (bits) of visited cities and of positions past K
-// become 0; bit t of the result is set where entry t stays non-zero.  Ids
+// this lane): bit t of the result is set where entry t is an unvisited city
+// (inside the first K positions); the weights (bits) of the others become 0.
+// Every unvisited entry is kept, a zero weight too: adding +0 changes no
+// running sum, and an entry whose sum does not rise is never the pick.  Ids
 // past K (-1 in the table) are replaced by city 0 so the lookup stays in the
 // list.
 template <bool PARTIAL>
 __device__ __forceinline__ unsigned rows_mask4(uint4 &wbits, uint2 &ip, int p0, int K,
-                                               const uint32_t *tw) {
-  int id[4] = {(int)(ip.x & 0xffffu), (int)(ip.x >> 16), (int)(ip.y & 0xffffu),
-               (int)(ip.y >> 16)};
+                                               const uint8_t *tb) {
+  uint32_t id[4] = {ip.x & 0xffffu, ip.x >> 16, ip.y & 0xffffu, ip.y >> 16};
   uint32_t wb[4] = {wbits.x, wbits.y, wbits.z, wbits.w};
-  unsigned nz = 0u;
+  unsigned keep = 0u;
 #pragma unroll
   for (int t = 0; t < 4; t++) {
-    if (PARTIAL && p0 + t >= K) id[t] = 0;
-    const bool seen = (tw[id[t] >> 5] >> (id[t] & 31)) & 1u;
-    if (seen || (PARTIAL && p0 + t >= K)) wb[t] = 0u;
-    nz |= ((wb[t] << 1) != 0u ? 1u : 0u) << t;  // non-zero (weights are never -0)
+    if (PARTIAL && p0 + t >= K) id[t] = 0u;
+    uint32_t m = (uint32_t)(int32_t)(int8_t)tb[id[t]];  // 0, or all ones if visited
+    if (PARTIAL && p0 + t >= K) m = ~0u;
+    wb[t] &= ~m;
+    keep |= ~m & (1u << t);
   }
   wbits = make_uint4(wb[0], wb[1], wb[2], wb[3]);
-  if (PARTIAL)
-    ip = make_uint2((uint32_t)id[0] | ((uint32_t)id[1] << 16),
-                    (uint32_t)id[2] | ((uint32_t)id[3] << 16));
-  return nz;
+  if (PARTIAL) ip = make_uint2(id[0] | (id[1] << 16), id[2] | (id[3] << 16));
+  return keep;
 }
 
 // Approximate pick of a row still in registers (one round of JB = 8 chunks
@@ -321,18 +335,13 @@ __device__ __forceinline__ int rows_guess_smem(const float *w, const int32_t *id
   }
   if (blk < 0) return -1;
   float acc = start;
-  const float4 *b4 = w4 + blk * 8;
+  const float *b1 = w + blk * 32;
+  const int key = blk & 3;
 #pragma unroll
-  for (int g = 0; g < 8; g++) {
-    const float4 v = b4[g];
-    acc = __fmaf_rn(v.x, 4 * g + 0 <= lane ? 1.0f : 0.0f, acc);
-    acc = __fmaf_rn(v.y, 4 * g + 1 <= lane ? 1.0f : 0.0f, acc);
-    acc = __fmaf_rn(v.z, 4 * g + 2 <= lane ? 1.0f : 0.0f, acc);
-    acc = __fmaf_rn(v.w, 4 * g + 3 <= lane ? 1.0f : 0.0f, acc);
-  }
+  for (int e = 0; e < 32; e++) acc = __fmaf_rn(b1[e ^ key], e <= lane ? 1.0f : 0.0f, acc);
   const unsigned hit = __ballot_sync(kFull, blk * 32 + lane < cnt && acc > rnd);
   if (!hit) return -1;
-  return id[blk * 32 + __ffs(hit) - 1];
+  return id[rows_swz(blk * 32 + __ffs(hit) - 1)];
 }
 
 struct RowsScan {
@@ -382,9 +391,9 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
       nz[j] = 0u;
       if (c0 < K) {  // warp-uniform
         if (c0 + 128 <= K)
-          nz[j] = rows_mask4<false>(q[j], ip[j], c0 + lane * 4, K, ra.tw);
+          nz[j] = rows_mask4<false>(q[j], ip[j], c0 + lane * 4, K, ra.tb);
         else
-          nz[j] = rows_mask4<true>(q[j], ip[j], c0 + lane * 4, K, ra.tw);
+          nz[j] = rows_mask4<true>(q[j], ip[j], c0 + lane * 4, K, ra.tb);
       } else {
         q[j] = make_uint4(0, 0, 0, 0);
       }
@@ -402,24 +411,28 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
       off[j] = __popc(b0 & lt) + 2 * __popc(b1 & lt) + 4 * __popc(b2 & lt);
       tot[j] = __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
     }
+    // Every entry is stored (no branch): a kept one at its place, a dropped
+    // one at this lane's sink slot past any chain length.
+    const int sink = ra.S - 32 + lane;
 #pragma unroll
     for (int j = 0; j < JB; j++) {
-      int o = r.cnt + off[j];
+      const int o = r.cnt + off[j];
+      const unsigned kp = nz[j];
+      const int rk[4] = {0, (int)(kp & 1u), (int)(kp & 1u) + (int)((kp >> 1) & 1u),
+                         __popc(kp & 7u)};
       const uint32_t wb[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
       const int id[4] = {(int)(ip[j].x & 0xffffu), (int)(ip[j].x >> 16),
                          (int)(ip[j].y & 0xffffu), (int)(ip[j].y >> 16)};
 #pragma unroll
       for (int t = 0; t < 4; t++) {
-        if ((nz[j] >> t) & 1u) {
-          wo[o] = __uint_as_float(wb[t]);
-          io[o] = id[t];
-          o++;
-        }
+        const int e = rows_swz(((kp >> t) & 1u) ? o + rk[t] : sink);
+        wo[e] = __uint_as_float(wb[t]);
+        io[e] = id[t];
       }
       r.cnt += tot[j];
     }
   }
-  for (int i = r.cnt + lane; i < L; i += 32) wo[i] = 0.0f;
+  for (int i = r.cnt + lane; i < L; i += 32) wo[rows_swz(i)] = 0.0f;
   if (u >= 0.0f && K > JB * 128) {
     __syncwarp();
     r.guess = rows_guess_smem<2>(wo, io, r.cnt, u, lane);
@@ -450,18 +463,20 @@ __device__ __forceinline__ int rows_exact(const float *pf, const float *bend, in
   }
   if (blk < 0) return -1;
   const int i = blk * 32 + lane;
-  const float v = pf[i];
+  const float v = pf[rows_swz(i)];
   const unsigned hit = __ballot_sync(kFull, i < cnt && (v > rnd || nan));
   return hit ? blk * 32 + __ffs(hit) - 1 : -1;
 }
 
-__device__ __forceinline__ void tw_set(uint32_t *tw, int city, bool on, int lane) {
+// Marks (or unmarks) a city in both tabu forms.
+__device__ __forceinline__ void tw_set(uint32_t *tw, uint8_t *tb, int city, bool on, int lane) {
   __syncwarp();
   if (lane == 0) {
     if (on)
       tw[city >> 5] |= 1u << (city & 31);
     else
       tw[city >> 5] &= ~(1u << (city & 31));
+    tb[city] = on ? 0xffu : 0u;
   }
   __syncwarp();
 }
@@ -472,26 +487,28 @@ __device__ __forceinline__ bool tw_test(const uint32_t *tw, int city) {
 
 // ---- chain warp --------------------------------------------------------------
 
+// Adds one block of 32 entries (slot g, logical component t at physical
+// component t ^ KEY) and writes each running sum where its weight was.
+template <int KEY>
 __device__ __forceinline__ void rows_chain_add32(float4 *w4, const float4 (&a)[8], float &s) {
 #pragma unroll
   for (int g = 0; g < 8; g++) {
-    float4 p;
-    s = __fadd_rn(s, a[g].x);
-    p.x = s;
-    s = __fadd_rn(s, a[g].y);
-    p.y = s;
-    s = __fadd_rn(s, a[g].z);
-    p.z = s;
-    s = __fadd_rn(s, a[g].w);
-    p.w = s;
-    w4[g] = p;
+    const float in[4] = {a[g].x, a[g].y, a[g].z, a[g].w};
+    float out[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      s = __fadd_rn(s, in[t ^ KEY]);
+      out[t ^ KEY] = s;
+    }
+    w4[g] = make_float4(out[0], out[1], out[2], out[3]);
   }
 }
 
 // Lane a < A: the running sums of ant a's buffer w over L entries (a multiple
 // of 32, zero-padded past its count), each written over its weight, the sum
-// at the end of every 32 entries in bend, the total in *S.  Two blocks of 32
-// per trip, each block's weights read while the previous block is added.
+// at the end of every 32 entries in bend, the total in *S.  Four blocks of
+// 32 per trip (their swizzle keys 0..3), each block's weights read while the
+// previous block is added.
 __device__ __forceinline__ void rows_chain(float *w, float *bend, int L, float *S) {
   float4 *w4 = reinterpret_cast<float4 *>(w);
   const int nb = L >> 5;
@@ -501,21 +518,23 @@ __device__ __forceinline__ void rows_chain(float *w, float *bend, int L, float *
 #pragma unroll
     for (int g = 0; g < 8; g++) a[g] = w4[g];
   }
-#pragma unroll 1
-  for (int b = 0; b < nb; b += 2) {
-    const bool two = b + 1 < nb;
-    const int nx = two ? b + 1 : b;
-#pragma unroll
-    for (int g = 0; g < 8; g++) v[g] = w4[nx * 8 + g];
-    rows_chain_add32(w4 + b * 8, a, s);
-    bend[b] = s;
-    if (!two) break;
-    const int nx2 = b + 2 < nb ? b + 2 : b + 1;
-#pragma unroll
-    for (int g = 0; g < 8; g++) a[g] = w4[nx2 * 8 + g];
-    rows_chain_add32(w4 + (b + 1) * 8, v, s);
-    bend[b + 1] = s;
+#define ACO_CHAIN_BLOCK(KEY, CUR, NXT)                                     \
+  {                                                                        \
+    const int bb = b + KEY;                                                \
+    if (bb >= nb) break;                                                   \
+    const int nx = bb + 1 < nb ? bb + 1 : bb;                              \
+    _Pragma("unroll") for (int g = 0; g < 8; g++) NXT[g] = w4[nx * 8 + g]; \
+    rows_chain_add32<KEY>(w4 + bb * 8, CUR, s);                            \
+    bend[bb] = s;                                                          \
   }
+#pragma unroll 1
+  for (int b = 0; b < nb; b += 4) {
+    ACO_CHAIN_BLOCK(0, a, v)
+    ACO_CHAIN_BLOCK(1, v, a)
+    ACO_CHAIN_BLOCK(2, a, v)
+    ACO_CHAIN_BLOCK(3, v, a)
+  }
+#undef ACO_CHAIN_BLOCK
   *S = s;
 }
 
@@ -534,7 +553,7 @@ struct RowsCtl {
 // the CTA.  `region` holds the A per-ant regions; `phase` is this scan
 // warp's staging-mbarrier parity, carried across items.
 template <bool AGING, bool PLAN>
-__device__ void rows_item(const ColonyDev &c, int first, int count, unsigned char *region,
+__device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int count, unsigned char *region,
                           size_t ant_bytes, RowsCtl &ctl, uint32_t &phase) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int A = (blockDim.x >> 5) - 1;  // scan warps; warp A is the chain warp
@@ -590,6 +609,7 @@ __device__ void rows_item(const ColonyDev &c, int first, int count, unsigned cha
     bool ok = true;
     if (valid) {
       for (int i = lane; i < (n + 31) / 32; i += 32) ra.tw[i] = 0u;
+      for (int i = lane; i < (n + 15) / 16 * 4; i += 32) reinterpret_cast<uint32_t *>(ra.tb)[i] = 0u;
       akey = aco_ant_key(c.seed, iter, (uint32_t)k);
       start = __float2int_rz(__fmul_rn(aco_uniform_key(akey, 0u), __int2float_rn(n)));
       if (start >= n) {  // impossible for u < 1; recorded, clamped
@@ -597,7 +617,7 @@ __device__ void rows_item(const ColonyDev &c, int first, int count, unsigned cha
         start = n - 1;
       }
       cur = start;
-      tw_set(ra.tw, start, true, lane);
+      tw_set(ra.tw, ra.tb, start, true, lane);
       if (lane == 0) trow[0] = start;
       if (AGING && a.blend) a.meanc = c.mean[start];
       rows_stage(c, ra, start, a.blend, lane);
@@ -625,7 +645,7 @@ __device__ void rows_item(const ColonyDev &c, int first, int count, unsigned cha
       if (valid) {
         u = aco_uniform_key(akey, (uint32_t)x);
         if (guess >= 0) {  // its row was staged (x + 1 < n)
-          tw_set(ra.tw, guess, true, lane);
+          tw_set(ra.tw, ra.tb, guess, true, lane);
           const float gm = (AGING && a.blend) ? c.mean[guess] : 0.0f;
           rows_stage_wait(c, ra, phase);
           inflight = false;
@@ -646,9 +666,9 @@ __device__ void rows_item(const ColonyDev &c, int first, int count, unsigned cha
       if (valid) {
         const int L = rows_chain_len(K, n, x);
         const int i = rows_exact(ra.w(b), ra.bend, cnt, L, ctl.S[warp], u, lane);
-        int next = i >= 0 ? ra.id(b)[i] : -1;
+        int next = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
         const bool hit = staged && next >= 0 && next == guess;
-        if (staged && !hit) tw_set(ra.tw, guess, false, lane);  // undo the guess
+        if (staged && !hit) tw_set(ra.tw, ra.tb, guess, false, lane);  // undo the guess
         if (next < 0) {
           next = fallback_city(c, cur, ra.tw, a, lane);
           fallbacks++;
@@ -657,7 +677,7 @@ __device__ void rows_item(const ColonyDev &c, int first, int count, unsigned cha
           ok = false;  // no unvisited city, or a bad id: cannot happen
           next = cur;
         }
-        if (!hit) tw_set(ra.tw, next, true, lane);
+        if (!hit) tw_set(ra.tw, ra.tb, next, true, lane);
         if (lane == 0) trow[x] = next;
         if (AGING && a.blend) a.meanc = c.mean[next];
         if (hit) {

@@ -1,21 +1,30 @@
 """Throughput benchmark of the GB300 ACO engine.
 
-Workload (one "step" = one full iteration of the hot path: construction of
+Default workload (`--workload parity_batch8`; one "step" = one full
+iteration of the hot path for every instance of the batch: construction of
 every ant's tour, tour lengths and bests, evaporation + deposit, next
-choice-info): rank-based Ant System with ant aging, n = 1000 cities drawn
-from 20 Gaussian clusters (sigma 300) in [0,10000)^2, m = 1000 ants, w = 6,
-candidate lists k = 30, rho = 0.1, FP32 pheromone, deterministic deposit.
-Synthetic seeded instance (no TSPLIB file is read).
+choice-info): the reference's own algorithm -- the Ant System with ant
+aging, full-row roulette over the whole nn row in the order of its CPU
+quicksort, the libm heuristic, select_local_best as the fallback, tau0 =
+1e-6, the sequential (deterministic) deposit -- on a batch of 8 instances of
+n = 1000 cities drawn from 20 Gaussian clusters (sigma 300) in
+[0,10000)^2, m = 1000 ants each, rho = 0.1, beta = 2.  Seeded synthetic
+instances (no TSPLIB file is read).  Before the timed steps the integer tour
+lengths of the first iterations of every instance are compared bit for bit
+with the CPU restatement of the reference path, and the result is printed
+in the line.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload parity_batch8|rbas_aging_n1000|batch512|large4096|learned]
 
 Prints one JSON line (rank 0).  `value` is tours/s over the device-timed
-steps (CUDA events on the colony's stream, L2 flushed between steps);
-`e2e` is the same metric through the public API from host buffers, the way
-the reference's TSP::execute drives a colony (create from the host distance
-matrix, initialize, per step constructSolution + the three getters, final
-getTour).  With --gpus N > 1 every rank runs an independent replica (the
-single-instance path does not shard; replicas only).
+steps (CUDA events on the batch's stream; the batch's working set, about
+370 MB, is larger than L2); `e2e` is the same metric through the public API
+from host buffers (create from host coordinates, initialize, per step one
+iteration and a read of every instance's best length).  `--impl reference`
+times the reference's CPU algorithm (its restatement in C, all host
+threads) on the identical configuration.  With --gpus N > 1 every rank runs
+its own batch of 8 instances (weak scaling; no collective on the data path).
 """
 import argparse
 import json
@@ -41,10 +50,53 @@ L2_FLUSH_BYTES = 256 << 20
 REF_BUDGET_S = 60.0  # CPU time the reference arm spends on its timed sample
 # Default timed steps per workload: about a second of timed work for the
 # single-colony lines (clock samples every 200 ms fall inside it).
-DEFAULT_STEPS = {"rbas_aging_n1000": 2000, "large4096": 300, "batch512": 10, "learned": 0}
+DEFAULT_STEPS = {"parity_batch8": 12, "rbas_aging_n1000": 2000, "large4096": 300,
+                 "batch512": 10, "learned": 0}
+# Parity-mode batch: the reference's own algorithm on 8 clustered n = 1000
+# instances (see the module docstring).
+PARITY_COUNT, PARITY_N, PARITY_SEED0 = 8, 1000, 2026
+PARITY_CHECK_ITERS = 2  # iterations of every instance checked against the port before timing
+PARITY_WORKLOAD = ("reference algorithm (Ant System with aging, full-row roulette in the "
+                   "reference nn order, libm heuristic, select_local_best fallback, tau0 1e-6, "
+                   "sequential deposit), batch of 8 instances of n=1000 (20 Gaussian clusters, "
+                   "sigma 300, [0,10000)^2), m=1000 each, rho=0.1, beta=2")
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parity_params():
+    """The reference's own configuration (AntSystem with aging,
+    src/AntSystem.cu:160-182; defaults inc/default.h) in parity mode."""
+    from acogpu_gb300 import _abi
+    return _abi.default_params(
+        num_ants=PARITY_N, variant=_abi.ACO_ANT_SYSTEM, aging=1, cand_k=0, rho=RHO, beta=BETA,
+        nn_order=_abi.ACO_NN_REFERENCE_QSORT, heuristic=_abi.ACO_HEURISTIC_LIBM,
+        fallback=_abi.ACO_FALLBACK_REFERENCE, tau0_mode=_abi.ACO_TAU0_REFERENCE,
+        deposit=_abi.ACO_DEPOSIT_DETERMINISTIC, seed=1234)
+
+
+def parity_instances(rank=0):
+    from acogpu_gb300 import instances
+    return [instances.clustered_instance(PARITY_N, seed=PARITY_SEED0 + 100 * rank + i)
+            for i in range(PARITY_COUNT)]
+
+
+def parity_config():
+    """The config dict of both arms (identical, so the two lines compare)."""
+    return {"workload": PARITY_WORKLOAD, "instances": PARITY_COUNT, "n": PARITY_N,
+            "m": PARITY_N, "k": PARITY_N, "variant": "AS", "aging": True, "rho": RHO,
+            "beta": BETA, "nn_order": "reference quicksort", "heuristic": "libm powf",
+            "fallback": "select_local_best", "tau0": 1e-6, "deposit": "sequential",
+            "iterations_per_step": 1}
+
+
+def instance_params(p, i):
+    """Parameters of instance i of a batch (aco_batch_create: seed + i * golden)."""
+    from acogpu_gb300 import _abi
+    q = _abi.AcoParams.from_buffer_copy(p)
+    q.seed = (p.seed + i * 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    return q
 
 
 def workload_params():
@@ -327,6 +379,195 @@ def run_ours(args, rank, world, local):
     }
 
 
+def parity_check(batch, insts, p, iters):
+    """Runs `iters` iterations of a fresh batch and of the CPU restatement of
+    the reference path on every instance; returns (all integer tour lengths
+    equal, tours compared)."""
+    import oracle
+    from acogpu_gb300 import instances
+    ports = []
+    for i, (x, y) in enumerate(insts):
+        q = oracle.Port(instance_params(p, i), instances.euc2d_distances(x, y),
+                        threads=os.cpu_count() or 1)
+        q.initialize()
+        ports.append(q)
+    same, compared = True, 0
+    for _ in range(iters):
+        batch.run(1)
+        batch.synchronize()
+        for i, q in enumerate(ports):
+            q.iterate()
+            g = batch.colony(i).tour_lengths()
+            same = same and bool(np.array_equal(g, q.lengths()))
+            compared += int(q.num_valid())
+    for q in ports:
+        q.close()
+    return same, compared
+
+
+def rows_bytes(n, tours):
+    """Algorithmic bytes of the long-row construction: per ant-step one
+    candidate row staged (n choice values and n int16 ids) and the tour
+    write."""
+    return tours * (n - 1) * (6 * n + 4)
+
+
+def run_parity(args, rank, world, local):
+    """The parity-mode batch (the reference's own algorithm), device-timed and
+    end to end; 8 instances per GPU (weak scaling)."""
+    import torch
+    import acogpu_gb300 as aco
+    torch.cuda.set_device(local)
+    insts = parity_instances(rank)
+    p = parity_params()
+    p.seed = distrib.replica_seed(1234, rank)
+    # ---- bit-exact check of the first iterations against the CPU path
+    b = aco.Batch(insts, params=p, num_ants=PARITY_N)
+    b.initialize()
+    checked, compared = parity_check(b, insts, p, PARITY_CHECK_ITERS) if rank == 0 else (None, 0)
+    b.run(max(0, args.warmup - PARITY_CHECK_ITERS))
+    b.synchronize()
+    built0, launches0 = b.tours_built(), b.launch_count()
+    fb0 = sum(b.colony(i).stats()["fallbacks"] for i in range(len(insts)))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            ev[i][0].record()
+            b.run(1)
+            b.synchronize()
+            ev[i][1].record()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    dev_s = sum(a.elapsed_time(e) for a, e in ev) / 1e3
+    tours = b.tours_built() - built0
+    launches = b.launch_count() - launches0
+    fallbacks = sum(b.colony(i).stats()["fallbacks"] for i in range(len(insts))) - fb0
+    # Construction alone, event-timed on the batch's stream by the library
+    # (the autotuner's timing runs reset the instances afterwards).
+    tune = b.autotune()
+    b.close()
+    # ---- end to end through the public API, host buffers
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e = aco.Batch(insts, params=p, num_ants=PARITY_N)
+    e.initialize()
+    d2h = 0
+    for _ in range(args.steps):
+        e.run(1)
+        e.glob_best()
+        d2h += 8 * len(insts)
+    e_built = e.tours_built()
+    e.synchronize()
+    e_wall = time.perf_counter() - t0
+    e.close()
+    (dev_s, e_wall), (tours_all, e_tours_all, launches) = distrib.reduce_times_and_counts(
+        [dev_s, e_wall], [tours, e_built, launches], device=torch.device("cuda", local))
+    if rank != 0:
+        return None
+    hbm = peaks().get("hbm_gbs")
+    per_launch = rows_bytes(PARITY_N, tours / args.steps)
+    construct_s = tune["construct_ms"] / 1e3
+    achieved = per_launch / construct_s / 1e9 if construct_s > 0 else None
+    return {
+        "metric": "tours/s", "value": tours_all / dev_s, "unit": "tours/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": dict(parity_config(),
+                       l2="working set about 370 MB per GPU, larger than L2"),
+        "ant_steps_per_s": tours_all * (PARITY_N - 1) / dev_s,
+        "parity": {"integer_tour_lengths_bit_exact": checked,
+                   "iterations_checked_per_instance": PARITY_CHECK_ITERS,
+                   "tours_compared": compared,
+                   "against": "C restatement of the reference CPU path (oracle/aco_oracle.c)"},
+        "fallback_rate": fallbacks / max(1, tours * (PARITY_N - 1)),
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_batch_construct_rows", "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if (hbm and achieved) else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm else None,
+                     "algorithmic_bytes_per_launch": per_launch,
+                     "construct_ms": tune["construct_ms"],
+                     "traffic": profiled_traffic("construct_rows_parity_batch8.md"),
+                     "traffic_source": "profiles/construct_rows_parity_batch8.md (ncu)"},
+        "e2e": {"value": e_tours_all / e_wall, "unit": "tours/s",
+                "h2d_bytes_per_step": 8 * PARITY_N * PARITY_COUNT / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps},
+        "clocks": clk.summary(),
+    }
+
+
+def parity_cpu_baseline(threads=None, iters=1):
+    """The CPU restatement on this host's cores: one instance of the batch, a
+    bounded sample of iterations."""
+    import oracle
+    from acogpu_gb300 import instances
+    threads = threads or os.cpu_count() or 1
+    x, y = parity_instances(0)[0]
+    q = oracle.Port(instance_params(parity_params(), 0), instances.euc2d_distances(x, y),
+                    threads=threads)
+    q.initialize()
+    t0 = time.perf_counter()
+    q.iterate(iters)
+    dt = time.perf_counter() - t0
+    tours = iters * q.num_valid()
+    q.close()
+    return {"value": tours / dt, "unit": "tours/s", "cores": threads, "kind": "port",
+            "sample": f"{iters} iteration(s) of instance 0 of the batch (from its start), "
+                      f"construction spread over {threads} threads"}
+
+
+def run_reference_parity(args, rank):
+    """Reference arm on the parity workload: the reference CPU algorithm (its
+    restatement in C) on the same 8 instances, all host threads; a bounded
+    sample of iterations, round-robin over the instances."""
+    if rank != 0:
+        return None
+    import oracle
+    from acogpu_gb300 import instances
+    threads = os.cpu_count() or 1
+    insts = parity_instances(0)
+    p = parity_params()
+    ports = []
+    for i, (x, y) in enumerate(insts):
+        q = oracle.Port(instance_params(p, i), instances.euc2d_distances(x, y), threads=threads)
+        q.initialize()
+        ports.append(q)
+    for w in range(args.warmup):
+        ports[w % len(ports)].iterate()
+    tours, done = 0, 0
+    t0 = time.perf_counter()
+    while done < args.steps * len(ports):
+        q = ports[done % len(ports)]
+        q.iterate()
+        tours += q.num_valid()
+        done += 1
+        if time.perf_counter() - t0 > REF_BUDGET_S:
+            break
+    dt = time.perf_counter() - t0
+    for q in ports:
+        q.close()
+    v = tours / dt
+    return {"metric": "tours/s", "value": v, "unit": "tours/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt * len(ports) / max(1, done), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(parity_config(),
+                           l2="working set about 370 MB per GPU, larger than L2"),
+            "cpu_baseline": {"value": v, "unit": "tours/s", "cores": threads, "kind": "port",
+                             "sample": f"{done} instance-iterations of the {args.steps} x "
+                                       f"{len(ports)} requested (at most {REF_BUDGET_S:.0f} s), "
+                                       f"after {args.warmup} warm-up, C restatement of the "
+                                       f"reference CPU path, {threads} threads"},
+            "e2e": {"value": v, "unit": "tours/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
 BATCH_COUNT, BATCH_CAP, BATCH_K = 512, 1024, 20
 BATCH_WORKLOAD = ("512 instances, n log-uniform in [50,2000] (uniform and clustered alternating), "
                   "m = min(n, 1024), k=20, AS, rho=0.1, beta=2; one persistent construction "
@@ -601,8 +842,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="rbas_aging_n1000",
-                    choices=("rbas_aging_n1000", "batch512", "learned", "large4096"))
+    ap.add_argument("--workload", default="parity_batch8",
+                    choices=("parity_batch8", "rbas_aging_n1000", "batch512", "learned",
+                             "large4096"))
     ap.add_argument("--train-instances", type=int, default=1024)
     ap.add_argument("--train-iters", type=int, default=200)
     ap.add_argument("--eval-instances", type=int, default=256)
@@ -613,7 +855,8 @@ def main():
         args.steps = DEFAULT_STEPS[args.workload]
     world, rank, local = dist_env()
     if args.impl == "reference":
-        out = run_reference(args, rank)
+        out = (run_reference_parity(args, rank) if args.workload == "parity_batch8"
+               else run_reference(args, rank))
         if out is not None:
             print(json.dumps(out), flush=True)
         return
@@ -623,12 +866,14 @@ def main():
         torch.distributed.init_process_group("nccl")
     try:
         fn = {"batch512": run_batch, "learned": run_learned, "large4096": run_large,
-              "rbas_aging_n1000": run_ours}[args.workload]
+              "rbas_aging_n1000": run_ours, "parity_batch8": run_parity}[args.workload]
         out = fn(args, rank, world, local)
         if out is not None:
             # the CPU baseline: rank 0 of a one-GPU run only
             if fn is run_ours and not args.no_cpu_baseline and world == 1:
                 out["cpu_baseline"] = cpu_baseline()
+            if fn is run_parity and not args.no_cpu_baseline and world == 1:
+                out["cpu_baseline"] = parity_cpu_baseline()
             print(json.dumps(out), flush=True)
     finally:
         if world > 1:

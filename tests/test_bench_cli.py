@@ -19,9 +19,10 @@ def run_main(monkeypatch, capsys, argv):
             return {"metric": "tours/s", "value": 1.0, "workload": name}
         return run
 
-    for name in ("run_ours", "run_batch", "run_learned", "run_large"):
+    for name in ("run_ours", "run_batch", "run_learned", "run_large", "run_parity"):
         monkeypatch.setattr(bench, name, fake(name))
     monkeypatch.setattr(bench, "cpu_baseline", lambda: {"value": 2.0, "kind": "port"})
+    monkeypatch.setattr(bench, "parity_cpu_baseline", lambda: {"value": 3.0, "kind": "port"})
     monkeypatch.setattr(sys, "argv", ["bench.py"] + argv)
     for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
         monkeypatch.delenv(k, raising=False)
@@ -33,8 +34,28 @@ def run_main(monkeypatch, capsys, argv):
 
 def test_headline_line_carries_the_cpu_baseline(monkeypatch, capsys):
     out, args = run_main(monkeypatch, capsys, [])
-    assert out["workload"] == "run_ours" and out["cpu_baseline"]["kind"] == "port"
-    assert args.steps == bench.DEFAULT_STEPS["rbas_aging_n1000"] and args.warmup >= 3
+    assert out["workload"] == "run_parity" and out["cpu_baseline"]["value"] == 3.0
+    assert args.steps == bench.DEFAULT_STEPS["parity_batch8"] and args.warmup >= 3
+
+
+def test_single_colony_line_carries_its_cpu_baseline(monkeypatch, capsys):
+    out, args = run_main(monkeypatch, capsys, ["--workload", "rbas_aging_n1000"])
+    assert out["workload"] == "run_ours" and out["cpu_baseline"]["value"] == 2.0
+    assert args.steps == bench.DEFAULT_STEPS["rbas_aging_n1000"]
+
+
+def test_both_arms_share_the_parity_config():
+    """The reference arm and the GPU arm print the same config dict."""
+    import inspect
+    src_ref = inspect.getsource(bench.run_reference_parity)
+    src_gpu = inspect.getsource(bench.run_parity)
+    for src in (src_ref, src_gpu):
+        assert "dict(parity_config()" in src
+    p = bench.parity_params()
+    from acogpu_gb300 import _abi
+    assert p.cand_k == 0 and p.nn_order == _abi.ACO_NN_REFERENCE_QSORT
+    assert p.heuristic == _abi.ACO_HEURISTIC_LIBM and p.fallback == _abi.ACO_FALLBACK_REFERENCE
+    assert p.tau0_mode == _abi.ACO_TAU0_REFERENCE and p.aging == 1
 
 
 def test_no_cpu_baseline_flag(monkeypatch, capsys):
