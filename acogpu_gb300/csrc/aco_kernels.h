@@ -81,9 +81,10 @@ cudaError_t launch_construct_cluster(const ColonyDev &c, int grid, int warps, in
 // CTA holds A <= kRowsMaxAnts ants of one instance, one scan warp per ant and
 // one chain warp (k_construct_rows.cu).  Each ant has a region of
 // rows_ant_bytes in shared memory (rows_layout): two buffers of compacted
-// weights and int32 ids (S = rows_slots(K) entries each), the running sums at
+// weights and int16 ids (S = rows_slots(K) entries each), the running sums at
 // every 32nd entry, a staging area for one row copied by TMA (pitch P = ldk:
-// choice or tau, eta, int16 ids), the tabu bits and a visited byte per city.
+// choice values, or tau for an ant that blends its fitness, and int16 ids),
+// the tabu bits and a visited byte per city.
 // The last 32 slots of each buffer are per-lane sinks for the stores of
 // dropped entries (past any chain length).  With aging,
 // launch_construct_rows runs the aging plan first (two launches).
@@ -92,16 +93,15 @@ constexpr int kRowsMaxAnts = 11;
 __host__ __device__ inline int rows_slots(int K) { return (K + 31) / 32 * 32 + 32; }
 struct RowsLayout {
   int S;
-  size_t id_off, bend_off, sw_off, se_off, si_off, tw_off, tb_off, bytes;
+  size_t id_off, bend_off, sw_off, si_off, tw_off, tb_off, bytes;
 };
 __host__ __device__ inline RowsLayout rows_layout(int n, int K, int P) {
   RowsLayout L;
   L.S = rows_slots(K);
   L.id_off = (size_t)L.S * 8;
-  L.bend_off = (size_t)L.S * 16;
+  L.bend_off = (size_t)L.S * 12;
   L.sw_off = L.bend_off + ((size_t)L.S / 32 * 4 + 15) / 16 * 16;
-  L.se_off = L.sw_off + (size_t)P * 4;
-  L.si_off = L.se_off + (size_t)P * 4;
+  L.si_off = L.sw_off + (size_t)P * 4;
   L.tw_off = L.si_off + ((size_t)P * 2 + 15) / 16 * 16;
   L.tb_off = L.tw_off + (size_t)(((n + 31) / 32 + 3) / 4) * 16;
   L.bytes = L.tb_off + (size_t)(n + 15) / 16 * 16;

@@ -1125,7 +1125,7 @@ int aco_batch_create(const aco_params *params, int32_t count, const int32_t *siz
                 (size_t)b->max_smem_optin;
   for (aco_colony *c : b->cols)
     if (!c->nn16) b->rows = false;
-  if (b->rows) b->apb = std::min(b->apb, kRowsMaxAnts);
+  if (b->rows) b->apb = kRowsMaxAnts;  // as many ants a CTA as the registers allow
   while (b->rows && b->apb > 1 &&
          batch_rows_smem_bytes(b->max_n, b->max_ldk_rows, b->apb) + 1024 >
              (size_t)b->max_smem_optin)

@@ -19,9 +19,9 @@
 // the same step, and A + 1 warps:
 //
 //  * scan warp a (one per ant): one lane copies the row it needs (choice
-//    values, or tau and eta for an ant that blends its fitness, and the int16
-//    city ids) into the ant's staging area with TMA bulk copies on an
-//    mbarrier; the warp then zeroes the weights of visited cities (a bit per
+//    values, or tau for an ant that blends its fitness -- it reads eta from
+//    L2 -- and the int16 city ids) into the ant's staging area with TMA bulk
+//    copies on an mbarrier; the warp then zeroes the weights of visited cities (a bit per
 //    city in shared memory) and compacts the non-zero weights, in row order,
 //    into one of the ant's two buffers (a lane's offset is the count of the
 //    lanes before it, from three ballots of the count bits);
@@ -66,10 +66,10 @@ namespace aco {
 // S = rows_slots(K), P = ldk:
 //   w[2]:  2 x S f32        compacted weights (two buffers); the chain warp
 //                           overwrites each weight with the running sum
-//   id[2]: 2 x S int32      their city ids
+//   id[2]: 2 x S int16      their city ids
 //   bend:  S/32 f32         running sum at the end of every 32 entries
-//   sw:    P f32            staged row: choice values (or tau)
-//   se:    P f32            staged row: eta (aging blend)
+//   sw:    P f32            staged row: choice values, or tau for an ant that
+//                           blends its fitness (which reads eta from L2)
 //   si:    P int16          staged row: city ids
 //   tw:    tabu bits        visited cities, 32 a word (words padded to 4; the
 //                           fallback's scans read them)
@@ -87,17 +87,16 @@ namespace aco {
 // blocks undoes it with a fixed permutation.
 struct RowsAnt {
   float *w0;
-  int32_t *id0;
+  int16_t *id0;
   float *bend;
   float *sw;
-  float *se;
   int16_t *si;
   uint32_t *tw;
   uint8_t *tb;
   uint64_t *bar;
   int S;
   __device__ __forceinline__ float *w(int b) const { return w0 + b * S; }
-  __device__ __forceinline__ int32_t *id(int b) const { return id0 + b * S; }
+  __device__ __forceinline__ int16_t *id(int b) const { return id0 + b * S; }
 };
 
 __device__ __forceinline__ RowsAnt rows_ant_at(unsigned char *base, int n, int K, int P,
@@ -106,10 +105,9 @@ __device__ __forceinline__ RowsAnt rows_ant_at(unsigned char *base, int n, int K
   RowsAnt r;
   r.S = L.S;
   r.w0 = reinterpret_cast<float *>(base);
-  r.id0 = reinterpret_cast<int32_t *>(base + L.id_off);
+  r.id0 = reinterpret_cast<int16_t *>(base + L.id_off);
   r.bend = reinterpret_cast<float *>(base + L.bend_off);
   r.sw = reinterpret_cast<float *>(base + L.sw_off);
-  r.se = reinterpret_cast<float *>(base + L.se_off);
   r.si = reinterpret_cast<int16_t *>(base + L.si_off);
   r.tw = reinterpret_cast<uint32_t *>(base + L.tw_off);
   r.tb = base + L.tb_off;
@@ -147,13 +145,8 @@ __device__ __forceinline__ void rows_stage(const ColonyDev &c, const RowsAnt &ra
     fence_proxy_async();  // the area's earlier generic-proxy reads come first
     const size_t off = (size_t)city * c.ldk;
     const uint32_t wb = (uint32_t)c.ldk * 4u, ib = (uint32_t)c.ldk * 2u;
-    mbar_arrive_expect_tx(ra.bar, (blend ? 2u * wb : wb) + ib);
-    if (!blend) {
-      tma_load_1d(ra.sw, c.choice_nn + off, wb, ra.bar);
-    } else {
-      tma_load_1d(ra.sw, c.tau_nn + off, wb, ra.bar);
-      tma_load_1d(ra.se, c.eta_nn + off, wb, ra.bar);
-    }
+    mbar_arrive_expect_tx(ra.bar, wb + ib);
+    tma_load_1d(ra.sw, (blend ? c.tau_nn : c.choice_nn) + off, wb, ra.bar);
     tma_load_1d(ra.si, c.nn16 + off, ib, ra.bar);
   }
 }
@@ -236,12 +229,13 @@ __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2
     const float y = __shfl_up_sync(kFull, inc, o);
     if (lane >= o) inc += y;
   }
+  // No early return below: every shuffle runs in every case, so the guess's
+  // instructions can interleave with the caller's compaction stores.
   const float S = __shfl_sync(kFull, inc, 28);
-  if (!(S > 0.0f) || !(S < INFINITY)) return -1;
+  const bool s_ok = S > 0.0f && S < INFINITY;
   const float rnd = u * S;
   const unsigned hc = __ballot_sync(kFull, (lane & 3) == 0 && inc > rnd);
-  if (!hc) return -1;
-  const int l0 = __ffs(hc) - 1;  // 4 * chunk
+  const int l0 = hc ? __ffs(hc) - 1 : 0;  // 4 * chunk
   const int js = l0 >> 2;
   const float base = __shfl_sync(kFull, inc - t1, l0);
   float x = ls[0];
@@ -263,8 +257,7 @@ __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2
   }
   incl += base;
   const unsigned hit = __ballot_sync(kFull, incl > rnd);
-  if (!hit) return -1;
-  const int l = __ffs(hit) - 1;
+  const int l = hit ? __ffs(hit) - 1 : 0;
   const float w[4] = {__uint_as_float(qq.x), __uint_as_float(qq.y), __uint_as_float(qq.z),
                       __uint_as_float(qq.w)};
   const int id[4] = {(int)(ii.x & 0xffffu), (int)(ii.x >> 16), (int)(ii.y & 0xffffu),
@@ -274,9 +267,10 @@ __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2
 #pragma unroll
   for (int t = 0; t < 4; t++) {
     acc += w[t];
-    if (city < 0 && w[t] != 0.0f && acc > rnd) city = id[t];
+    city = (city < 0 && w[t] != 0.0f && acc > rnd) ? id[t] : city;
   }
-  return __shfl_sync(kFull, city, l);
+  city = __shfl_sync(kFull, city, l);
+  return (s_ok && hc && hit) ? city : -1;
 }
 
 // Approximate pick of a compacted buffer (rows of more than 128 JB entries):
@@ -286,7 +280,7 @@ __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2
 // masked-FMA prefixes from the block's approximate start.  NR rounds of 32
 // blocks (cnt <= 1024 NR).  Returns the city, or -1.
 template <int NR>
-__device__ __forceinline__ int rows_guess_smem(const float *w, const int32_t *id, int cnt, float u,
+__device__ __forceinline__ int rows_guess_smem(const float *w, const int16_t *id, int cnt, float u,
                                                int lane) {
   if (cnt <= 0 || cnt > 1024 * NR) return -1;
   const float4 *w4 = reinterpret_cast<const float4 *>(w);
@@ -355,10 +349,11 @@ struct RowsScan {
 // every chunk's visited lookups, then the ballots of every chunk, then the
 // compacting stores.
 template <int JB>
-__device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt &ra, bool blend,
-                                              float meanc, float ratio, float *wo, int32_t *io,
-                                              int L, float u, int lane) {
+__device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt &ra, int city,
+                                              bool blend, float meanc, float ratio, float *wo,
+                                              int16_t *io, int L, float u, int lane) {
   const int K = c.K;
+  const float *erow = c.eta_nn + (size_t)city * c.ldk;
   RowsScan r;
   r.cnt = 0;
   r.guess = -1;
@@ -377,7 +372,7 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
       } else {
         const float4 t = in ? *reinterpret_cast<const float4 *>(ra.sw + p0)
                             : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 e = in ? *reinterpret_cast<const float4 *>(ra.se + p0)
+        const float4 e = in ? __ldg(reinterpret_cast<const float4 *>(erow + p0))
                             : make_float4(0.f, 0.f, 0.f, 0.f);
         q[j].x = __float_as_uint(blend_fitness(t.x, e.x, meanc, ratio, c.use_alpha, c.alpha));
         q[j].y = __float_as_uint(blend_fitness(t.y, e.y, meanc, ratio, c.use_alpha, c.alpha));
@@ -421,8 +416,8 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
       const int rk[4] = {0, (int)(kp & 1u), (int)(kp & 1u) + (int)((kp >> 1) & 1u),
                          __popc(kp & 7u)};
       const uint32_t wb[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
-      const int id[4] = {(int)(ip[j].x & 0xffffu), (int)(ip[j].x >> 16),
-                         (int)(ip[j].y & 0xffffu), (int)(ip[j].y >> 16)};
+      const int16_t id[4] = {(int16_t)(ip[j].x & 0xffffu), (int16_t)(ip[j].x >> 16),
+                             (int16_t)(ip[j].y & 0xffffu), (int16_t)(ip[j].y >> 16)};
 #pragma unroll
       for (int t = 0; t < 4; t++) {
         const int e = rows_swz(((kp >> t) & 1u) ? o + rk[t] : sink);
@@ -479,6 +474,13 @@ __device__ __forceinline__ void tw_set(uint32_t *tw, uint8_t *tb, int city, bool
     tb[city] = on ? 0xffu : 0u;
   }
   __syncwarp();
+}
+
+// The fallback (rare): out of line, so its code stays out of the step loop's
+// instruction stream.
+__device__ __noinline__ int rows_fallback(const ColonyDev &c, int cur, const uint32_t *tw,
+                                          AntCtx a, int lane) {
+  return fallback_city(c, cur, tw, a, lane);
 }
 
 __device__ __forceinline__ bool tw_test(const uint32_t *tw, int city) {
@@ -622,7 +624,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       if (AGING && a.blend) a.meanc = c.mean[start];
       rows_stage(c, ra, start, a.blend, lane);
       rows_stage_wait(c, ra, phase);
-      const RowsScan r0 = rows_scan<8>(c, ra, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
+      const RowsScan r0 = rows_scan<8>(c, ra, start, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
                                        rows_chain_len(K, n, 1),
                                        n > 2 ? aco_uniform_key(akey, 1u) : -1.0f, lane);
       cnt = r0.cnt;
@@ -637,40 +639,52 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
     for (int x = 1; x < n; x++) {
       __syncwarp();
       named_bar_arrive(kBarRowsReady, threads);
-      RowsScan g;  // the guessed city's row, and the guess after it
+      // Pass 0 scans the guessed pick's row (while the chain runs), then finds
+      // the exact pick; pass 1 scans the real pick's row after a wrong or
+      // missing guess.  One call site of the scan serves both.
+      RowsScan g;
       g.cnt = 0;
       g.guess = -1;
-      bool staged = false;
+      int todo = -1;  // city whose row goes into buffer b ^ 1 in this pass
+      bool staged = false, hit = false;
+      int next = cur;
       float u = 0.0f;
       if (valid) {
         u = aco_uniform_key(akey, (uint32_t)x);
         if (guess >= 0) {  // its row was staged (x + 1 < n)
           tw_set(ra.tw, ra.tb, guess, true, lane);
-          const float gm = (AGING && a.blend) ? c.mean[guess] : 0.0f;
+          todo = guess;
+          staged = true;
+        }
+      }
+#pragma unroll 1
+      for (int pass = 0; pass < 2; pass++) {
+        if (todo >= 0) {
+          const float m = (AGING && a.blend) ? c.mean[todo] : 0.0f;
           rows_stage_wait(c, ra, phase);
           inflight = false;
-          g = rows_scan<8>(c, ra, a.blend, gm, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
+          g = rows_scan<8>(c, ra, todo, a.blend, m, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
                            rows_chain_len(K, n, x + 1),
                            x + 2 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : -1.0f, lane);
-          staged = true;
           if (g.guess >= 0 && x + 2 < n) {
             rows_stage(c, ra, g.guess, a.blend, lane);
             inflight = true;
           } else {
             g.guess = -1;
           }
+          todo = -1;
         }
-      }
-      __syncwarp();
-      named_bar_sync(kBarChainDone, threads);
-      if (valid) {
-        const int L = rows_chain_len(K, n, x);
-        const int i = rows_exact(ra.w(b), ra.bend, cnt, L, ctl.S[warp], u, lane);
-        int next = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
-        const bool hit = staged && next >= 0 && next == guess;
+        if (pass == 1) break;
+        __syncwarp();
+        named_bar_sync(kBarChainDone, threads);  // once per step, in pass 0
+        if (!valid) break;
+        const int i = rows_exact(ra.w(b), ra.bend, cnt, rows_chain_len(K, n, x), ctl.S[warp],
+                                 u, lane);
+        next = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
+        hit = staged && next >= 0 && next == guess;
         if (staged && !hit) tw_set(ra.tw, ra.tb, guess, false, lane);  // undo the guess
         if (next < 0) {
-          next = fallback_city(c, cur, ra.tw, a, lane);
+          next = rows_fallback(c, cur, ra.tw, a, lane);
           fallbacks++;
         }
         if ((unsigned)next >= (unsigned)n || (!hit && tw_test(ra.tw, next))) {
@@ -680,30 +694,19 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         if (!hit) tw_set(ra.tw, ra.tb, next, true, lane);
         if (lane == 0) trow[x] = next;
         if (AGING && a.blend) a.meanc = c.mean[next];
-        if (hit) {
-          cnt = g.cnt;
-          guess = g.guess;
-        } else {
+        if (!hit && x + 1 < n) {
           if (inflight) {  // the copy of a row no longer needed
             rows_stage_wait(c, ra, phase);
             inflight = false;
           }
-          guess = -1;
-          if (x + 1 < n) {
-            rows_stage(c, ra, next, a.blend, lane);
-            rows_stage_wait(c, ra, phase);
-            const RowsScan r = rows_scan<8>(
-                c, ra, a.blend, a.meanc, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
-                rows_chain_len(K, n, x + 1),
-                x + 2 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : -1.0f, lane);
-            cnt = r.cnt;
-            if (r.guess >= 0 && x + 2 < n) {
-              guess = r.guess;
-              rows_stage(c, ra, guess, a.blend, lane);
-              inflight = true;
-            }
-          }
+          rows_stage(c, ra, next, a.blend, lane);
+          inflight = true;
+          todo = next;
         }
+      }
+      if (valid) {
+        cnt = g.cnt;
+        guess = g.guess;
         cur = next;
       }
       b ^= 1;
