@@ -79,6 +79,48 @@ def make_case(c):
     return out, meta
 
 
+# The first configuration of the benchmark plan, run as specified: plain Ant
+# System, n = 100 cities with integer coordinates uniform in [0, 10000)^2,
+# m = 100 ants, alpha 1, beta 2, rho 0.5, full-row roulette, 1000
+# iterations, no aging.  Recorded as digests, not arrays.
+DIGEST = dict(name="c1_as_n100_1000iters", n=100, m=100, seed=100, beta=2.0, rho=0.5,
+              iters=1000, checkpoints=[1, 2, 10, 50, 100, 250, 500, 750, 1000])
+
+
+def chain_digest(h, tours, lengths, tau):
+    """Running SHA-256 over the iterations: h_i = H(h_{i-1} | tours | lengths | tau)."""
+    m = hashlib.sha256(h)
+    m.update(np.ascontiguousarray(tours, dtype=np.int32).tobytes())
+    m.update(np.ascontiguousarray(lengths, dtype=np.int64).tobytes())
+    m.update(np.ascontiguousarray(tau, dtype=np.float32).tobytes())
+    return m.digest()
+
+
+def digest_params(c):
+    return _abi.default_params(num_ants=c["m"], beta=c["beta"], rho=c["rho"], aging=0,
+                               seed=1000 + c["seed"], nn_order=_abi.ACO_NN_REFERENCE_QSORT)
+
+
+def make_digest(c):
+    """Per-iteration digest of the compiled reference over a whole run."""
+    x, y = instances.uniform_instance(c["n"], seed=c["seed"])
+    d = oracle.distances(x, y)
+    ref = oracle.Ref(digest_params(c), d)
+    ref.initialize()
+    h = b""
+    out = dict(c, iter_best=[], glob_best=[], digests={})
+    for it in range(1, c["iters"] + 1):
+        ref.iterate()
+        h = chain_digest(h, ref.tours(), ref.lengths(), ref.pheromone())
+        out["iter_best"].append(int(ref.iter_best()))
+        out["glob_best"].append(int(ref.glob_best()))
+        if it in c["checkpoints"]:
+            out["digests"][str(it)] = h.hex()
+    out["best_tour"] = [int(v) for v in ref.best_tour()]
+    ref.close()
+    return out
+
+
 def main():
     index = {}
     for c in CASES:
@@ -88,6 +130,10 @@ def main():
         print(c["name"], "glob_best", arrays["glob_best"][-1])
     with open(os.path.join(HERE, "cases.json"), "w") as f:
         json.dump(index, f, indent=1)
+    dg = make_digest(DIGEST)
+    with open(os.path.join(HERE, DIGEST["name"] + ".json"), "w") as f:
+        json.dump(dg, f)
+    print(DIGEST["name"], "glob_best", dg["glob_best"][-1])
 
 
 if __name__ == "__main__":

@@ -49,6 +49,45 @@ def test_port_matches_golden(name):
     assert np.array_equal(q.best_tour(), g["best_tour"])
 
 
+def c1_digest_case():
+    """The whole-run digest recorded from the compiled reference (C1: plain
+    AS, n = 100, m = 100, beta 2, rho 0.5, full rows, 1000 iterations)."""
+    return json.load(open(os.path.join(GOLDEN, "c1_as_n100_1000iters.json")))
+
+
+def c1_digest_params(c):
+    return _abi.default_params(num_ants=c["m"], beta=c["beta"], rho=c["rho"], aging=0,
+                               seed=1000 + c["seed"], nn_order=_abi.ACO_NN_REFERENCE_QSORT)
+
+
+def chain_digest(h, tours, lengths, tau):
+    m = hashlib.sha256(h)
+    m.update(np.ascontiguousarray(tours, dtype=np.int32).tobytes())
+    m.update(np.ascontiguousarray(lengths, dtype=np.int64).tobytes())
+    m.update(np.ascontiguousarray(tau, dtype=np.float32).tobytes())
+    return m.digest()
+
+
+def test_port_reproduces_the_whole_c1_run():
+    """All 1000 iterations of C1 on the port: every iteration's best, and the
+    running digest of tours, lengths and pheromone at the checkpoints, equal
+    the compiled reference's."""
+    c = c1_digest_case()
+    x, y = instances.uniform_instance(c["n"], seed=c["seed"])
+    q = oracle.Port(c1_digest_params(c), oracle.distances(x, y), threads=4)
+    q.initialize()
+    h = b""
+    for it in range(1, c["iters"] + 1):
+        q.iterate()
+        h = chain_digest(h, q.tours(), q.lengths(), q.pheromone())
+        assert q.iter_best() == c["iter_best"][it - 1], f"iteration {it}: iteration best"
+        assert q.glob_best() == c["glob_best"][it - 1], f"iteration {it}: best so far"
+        if str(it) in c["digests"]:
+            assert h.hex() == c["digests"][str(it)], f"iteration {it}: digest"
+    assert [int(v) for v in q.best_tour()] == c["best_tour"]
+    q.close()
+
+
 needs_ref = pytest.mark.skipif(not oracle.ref_available(), reason="reference sources absent")
 
 
