@@ -50,7 +50,7 @@ L2_FLUSH_BYTES = 256 << 20
 REF_BUDGET_S = 60.0  # CPU time the reference arm spends on its timed sample
 # Default timed steps per workload: about a second of timed work for the
 # single-colony lines (clock samples every 200 ms fall inside it).
-DEFAULT_STEPS = {"parity_batch8": 12, "rbas_aging_n1000": 2000, "large4096": 300,
+DEFAULT_STEPS = {"parity_batch8": 40, "rbas_aging_n1000": 2000, "large4096": 300,
                  "batch512": 10, "learned": 0}
 # Parity-mode batch: the reference's own algorithm on 8 clustered n = 1000
 # instances (see the module docstring).
@@ -455,7 +455,9 @@ def run_parity(args, rank, world, local):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e = aco.Batch(insts, params=p, num_ants=PARITY_N)
+    t_create = time.perf_counter() - t0
     e.initialize()
+    t_setup = time.perf_counter() - t0
     d2h = 0
     for _ in range(args.steps):
         e.run(1)
@@ -497,7 +499,8 @@ def run_parity(args, rank, world, local):
                      "traffic_source": "profiles/construct_rows_parity_batch8.md (ncu)"},
         "e2e": {"value": e_tours_all / e_wall, "unit": "tours/s",
                 "h2d_bytes_per_step": 8 * PARITY_N * PARITY_COUNT / args.steps,
-                "d2h_bytes_per_step": d2h / args.steps},
+                "d2h_bytes_per_step": d2h / args.steps, "create_s": t_create,
+                "setup_s": t_setup},
         "clocks": clk.summary(),
     }
 
@@ -592,6 +595,73 @@ def batch_params():
                                seed=4321)
 
 
+def batch_cpu_sample(iters=2, per_stratum=2, strata=8, budget_s=REF_BUDGET_S):
+    """The uneven batch on the CPU restatement, all host threads: a stratified
+    sample of instances (per_stratum from each of `strata` size bands), `iters`
+    iterations each after one warm-up, extrapolated to the whole batch by the
+    ant-steps it holds (sum of m (n - 1): with candidate lists a step costs
+    about the same at every n).  Returns (tours/s, description)."""
+    import oracle
+    from acogpu_gb300 import instances
+    threads = os.cpu_count() or 1
+    insts = batch_instances()
+    sizes = np.array([len(x) for x, _ in insts])
+    ants = np.minimum(sizes, BATCH_CAP)
+    order = np.argsort(sizes, kind="stable")
+    bands = np.array_split(order, strata)
+    picked = [int(b[(len(b) - 1) * j // max(1, per_stratum - 1)]) for b in bands
+              for j in range(per_stratum)]
+    t_s, steps_s = 0.0, 0.0
+    t_start = time.perf_counter()
+    for i in picked:
+        x, y = insts[i]
+        pi = instance_params(batch_params(), i)
+        pi.num_ants = int(ants[i])
+        q = oracle.Port(pi, instances.euc2d_distances(x, y), threads=threads)
+        q.initialize()
+        q.iterate(1)
+        t0 = time.perf_counter()
+        q.iterate(iters)
+        t_s += time.perf_counter() - t0
+        steps_s += iters * float(ants[i]) * (sizes[i] - 1)
+        q.close()
+        if time.perf_counter() - t_start > budget_s:
+            break
+    total_steps = float((ants * (sizes - 1)).sum())
+    t_batch = t_s / steps_s * total_steps  # seconds for one whole-batch iteration
+    v = float(ants.sum()) / t_batch
+    desc = (f"{len(picked)} of {len(insts)} instances (stratified by size, {per_stratum} from each "
+            f"of {strata} bands), {iters} iterations each after 1 warm-up, extrapolated to the "
+            f"whole batch by its ant-steps (sum of m(n-1)); C restatement, {threads} threads")
+    return v, threads, desc
+
+
+def run_reference_batch(args, rank):
+    """Reference arm on the uneven batch: the same rule (candidate lists of
+    20, best-choice fallback -- the reference itself has no candidate lists)
+    on the CPU restatement, from a stratified sample."""
+    if rank != 0:
+        return None
+    v, threads, desc = batch_cpu_sample()
+    return {"metric": "tours/s", "value": v, "unit": "tours/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": batch_config(BATCH_COUNT),
+            "cpu_baseline": {"value": v, "unit": "tours/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": v, "unit": "tours/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def batch_config(count):
+    sizes = np.array([len(x) for x, _ in batch_instances(count)])
+    return {"workload": BATCH_WORKLOAD, "instances": int(count),
+            "cities_total": int(sizes.sum()),
+            "ants_per_iteration": int(np.minimum(sizes, BATCH_CAP).sum()),
+            "l2": "working set 5+ GB, larger than L2"}
+
+
 def run_batch(args, rank, world, local):
     """Batched uneven instances: whole-batch iterations, device-timed.  On N
     GPUs, 512·N instances are generated and sharded by estimated cost (weak
@@ -649,9 +719,7 @@ def run_batch(args, rank, world, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": BATCH_WORKLOAD, "instances": len(allinst),
-                       "cities_total": int(sizes.sum()), "ants_per_iteration": int(ants.sum()),
-                       "l2": "working set 5+ GB, larger than L2"},
+            "config": batch_config(len(allinst)),
             "ant_steps_per_s": float((ants * (sizes - 1)).sum()) * args.steps / dev_s,
             "autotune": tune, "setup_s": setup_s, "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": "k_batch_construct", "achieved": achieved,
@@ -855,8 +923,12 @@ def main():
         args.steps = DEFAULT_STEPS[args.workload]
     world, rank, local = dist_env()
     if args.impl == "reference":
-        out = (run_reference_parity(args, rank) if args.workload == "parity_batch8"
-               else run_reference(args, rank))
+        if args.workload == "parity_batch8":
+            out = run_reference_parity(args, rank)
+        elif args.workload == "batch512":
+            out = run_reference_batch(args, rank)
+        else:
+            out = run_reference(args, rank)
         if out is not None:
             print(json.dumps(out), flush=True)
         return
@@ -874,6 +946,10 @@ def main():
                 out["cpu_baseline"] = cpu_baseline()
             if fn is run_parity and not args.no_cpu_baseline and world == 1:
                 out["cpu_baseline"] = parity_cpu_baseline()
+            if fn is run_batch and not args.no_cpu_baseline and world == 1:
+                v, threads, desc = batch_cpu_sample(iters=1, per_stratum=1)
+                out["cpu_baseline"] = {"value": v, "unit": "tours/s", "cores": threads,
+                                       "kind": "port", "sample": desc}
             print(json.dumps(out), flush=True)
     finally:
         if world > 1:

@@ -23,6 +23,7 @@ def run_main(monkeypatch, capsys, argv):
         monkeypatch.setattr(bench, name, fake(name))
     monkeypatch.setattr(bench, "cpu_baseline", lambda: {"value": 2.0, "kind": "port"})
     monkeypatch.setattr(bench, "parity_cpu_baseline", lambda: {"value": 3.0, "kind": "port"})
+    monkeypatch.setattr(bench, "batch_cpu_sample", lambda **kw: (4.0, 2, "sample"))
     monkeypatch.setattr(sys, "argv", ["bench.py"] + argv)
     for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
         monkeypatch.delenv(k, raising=False)
@@ -63,9 +64,14 @@ def test_no_cpu_baseline_flag(monkeypatch, capsys):
     assert "cpu_baseline" not in out
 
 
-@pytest.mark.parametrize("workload,fn", [("batch512", "run_batch"), ("large4096", "run_large"),
-                                         ("learned", "run_learned")])
+@pytest.mark.parametrize("workload,fn", [("large4096", "run_large"), ("learned", "run_learned")])
 def test_other_workloads(monkeypatch, capsys, workload, fn):
     out, args = run_main(monkeypatch, capsys, ["--workload", workload])
     assert out["workload"] == fn and "cpu_baseline" not in out
     assert args.steps == bench.DEFAULT_STEPS[workload]
+
+
+def test_batch_line_carries_the_sampled_cpu_baseline(monkeypatch, capsys):
+    out, args = run_main(monkeypatch, capsys, ["--workload", "batch512"])
+    assert out["workload"] == "run_batch" and out["cpu_baseline"]["value"] == 4.0
+    assert args.steps == bench.DEFAULT_STEPS["batch512"]
