@@ -23,9 +23,15 @@ cudaError_t launch_heuristic_table(const int32_t *dist, int n, int ld, const flo
 cudaError_t launch_nn_sort_stable(const int32_t *dist, int n, int ld, int K, int ldk, int32_t *nn,
                                   ColonyState *st, cudaStream_t s, int32_t *nn2 = nullptr,
                                   int t2 = 0);
-// The reference CPU quicksort permutation (full rows only).
+// The reference CPU quicksort permutation (full rows only): one thread per
+// row on a global scratch of n rows of ld int32, or (the _smem version) one
+// warp per row in shared memory; nn_ref_qsort_smem_rows gives the rows a CTA
+// holds within max_smem bytes (0: the row does not fit).
 cudaError_t launch_nn_ref_qsort(const int32_t *dist, int n, int ld, int32_t *scratch, int32_t *nn,
                                 int ldk, ColonyState *st, cudaStream_t s);
+int nn_ref_qsort_smem_rows(int n, int max_smem);
+cudaError_t launch_nn_ref_qsort_smem(const int32_t *dist, int n, int ld, int32_t *nn, int ldk,
+                                     ColonyState *st, int max_smem, cudaStream_t s);
 cudaError_t launch_gather_nn_f32(const float *src, int n, int ld, const int32_t *nn, int K,
                                  int ldk, float *dst, cudaStream_t s);
 cudaError_t launch_greedy_tau0(const ColonyDev &c, int tau0_mode, float tau0_value,

@@ -522,17 +522,26 @@ int aco_colony_initialize(aco_colony *c) {
                                       c->nn2, c->t2),
              "nn sort");
   } else {
+    // The sort runs in shared memory when a row fits (one warp per row),
+    // else on a global scratch (one thread per row); same permutation.
+    const bool smem_sort = nn_ref_qsort_smem_rows(n, c->max_smem_optin) >= 1;
     int32_t *scratch = nullptr, *full = nullptr;
-    ACO_CUDA(c, cudaMallocAsync(&scratch, (size_t)n * c->ld * 4, c->stream), "alloc scratch");
+    if (!smem_sort)
+      ACO_CUDA(c, cudaMallocAsync(&scratch, (size_t)n * c->ld * 4, c->stream), "alloc scratch");
     if (c->K == n) {
       full = c->nn;  // the sort writes n ids a row; the pitch's padding is -1
       ACO_CUDA(c, cudaMemsetAsync(c->nn, 0xff, (size_t)n * c->ldk * 4, c->stream), "memset nn");
     } else {
       ACO_CUDA(c, cudaMallocAsync(&full, (size_t)n * c->ld * 4, c->stream), "alloc scratch");
     }
-    ACO_CUDA(c, launch_nn_ref_qsort(c->dist, n, c->ld, scratch, full, c->K == n ? c->ldk : c->ld,
-                                    c->st, c->stream),
-             "nn quicksort");
+    if (smem_sort)
+      ACO_CUDA(c, launch_nn_ref_qsort_smem(c->dist, n, c->ld, full, c->K == n ? c->ldk : c->ld,
+                                           c->st, c->max_smem_optin, c->stream),
+               "nn quicksort");
+    else
+      ACO_CUDA(c, launch_nn_ref_qsort(c->dist, n, c->ld, scratch, full,
+                                      c->K == n ? c->ldk : c->ld, c->st, c->stream),
+               "nn quicksort");
     if (full != c->nn) {
       ACO_CUDA(c, cudaMemsetAsync(c->nn, 0xff, (size_t)n * c->ldk * 4, c->stream), "memset nn");
       ACO_CUDA(c, cudaMemcpy2DAsync(c->nn, (size_t)c->ldk * 4, full, (size_t)c->ld * 4,
@@ -548,7 +557,7 @@ int aco_colony_initialize(aco_colony *c) {
       }
       ACO_CUDA(c, cudaFreeAsync(full, c->stream), "free");
     }
-    ACO_CUDA(c, cudaFreeAsync(scratch, c->stream), "free");
+    if (scratch) ACO_CUDA(c, cudaFreeAsync(scratch, c->stream), "free");
   }
   ACO_CUDA(c, launch_gather_nn_f32(c->eta, n, c->ld, c->nn, c->K, c->ldk, c->eta_nn, c->stream),
            "eta_nn");
