@@ -29,7 +29,7 @@ ACO_CONSTRUCT_AUTO, ACO_CONSTRUCT_GLOBAL, ACO_CONSTRUCT_STAGED = 0, 1, 2
 ACO_CONSTRUCT_DIRECT, ACO_CONSTRUCT_CLUSTER = 3, 4
 ACO_CONSTRUCT_ROWS = 5
 ACO_FALLBACK_TIER_AUTO, ACO_FALLBACK_TIER_ON, ACO_FALLBACK_TIER_OFF = 0, 1, 2
-ACO_GEMM_MMA_SYNC, ACO_GEMM_TCGEN05 = 0, 1
+ACO_GEMM_MMA_SYNC, ACO_GEMM_TCGEN05, ACO_GEMM_FUSED = 0, 1, 2
 
 TIMER_NAMES = ("init_tour", "tour", "compute_ant_distance", "evaporate_pheromone",
                "update_pheromone", "compute_probabilities")

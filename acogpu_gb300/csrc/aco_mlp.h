@@ -46,9 +46,22 @@ cudaError_t launch_grad_hidden1(const float *dH1, const __nv_bfloat16 *H1, int E
                                 __nv_bfloat16 *dZt, int ldt, float *gb, cudaStream_t s);
 cudaError_t launch_transpose_feats(const __nv_bfloat16 *X, int E, __nv_bfloat16 *Xt, int ldt,
                                    cudaStream_t s);
-cudaError_t launch_adam(float *w, float *g, float *m1, float *m2, int count, float lr, float b1,
-                        float b2, float eps, float bc1, float bc2, __nv_bfloat16 *wb,
-                        __nv_bfloat16 *wbt, int rows, int cols, int ldb, cudaStream_t s);
+// The whole forward (and, with train, loss and backward) pass over `rows`
+// edges in one tcgen05 kernel (k_mlp_fused.cu); grid = mlp_fused_grid().
+// Training writes one partial row per CTA into part (ld >= kParamCount + 1,
+// a multiple of 4): the gradient in packed order, then the loss.
+int mlp_fused_grid(int rows, int sms);
+cudaError_t launch_mlp_fused(bool train, const __nv_bfloat16 *X, int rows,
+                             const __nv_bfloat16 *w1b, const __nv_bfloat16 *w2b,
+                             const __nv_bfloat16 *w2tb, const float *w, const float *labels,
+                             float pos_weight, float norm, float *out, float *part, int part_ld,
+                             int grid, uint32_t *err, cudaStream_t s);
+// Sums G partial rows in order into gout / loss_out and, with adam, applies
+// the Adam step and refreshes the BF16 weight copies.
+cudaError_t launch_mlp_reduce(float *part, int G, int ld, bool clear, float *gout, float *loss_out,
+                              bool adam, float *w, float *m1, float *m2, float lr, float b1,
+                              float b2, float eps, float bc1, float bc2, __nv_bfloat16 *w1b,
+                              __nv_bfloat16 *w2b, __nv_bfloat16 *w2tb, cudaStream_t s);
 cudaError_t launch_apply_prior(const ColonyDev &c, const float *prob, float floor_,
                                cudaStream_t s);
 

@@ -20,95 +20,23 @@
 
 #include "aco_kernels.h"
 #include "aco_mlp.h"
+#include "aco_tc.cuh"
 
 namespace aco {
 
 namespace {
 
-constexpr int kTcBM = 128, kTcBK = 64;
-
-// Bounded mbarrier wait (see mbar_wait_bounded) reporting into `err`.
-__device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t parity, uint32_t *err) {
-  for (uint32_t i = 0; i < kMaxPolls; i++)
-    if (mbar_try_wait(bar, parity)) return true;
-  if (err) atomicOr(err, kErrTimeout);
-  return false;
-}
-
-// Shared-memory descriptor of a K-major operand tile with 128-byte
-// swizzle: start address, stride between 8-row groups (1024 bytes),
-// descriptor version 1, layout type SWIZZLE_128B.
-__device__ __forceinline__ uint64_t smem_desc_sw128(const void *tile) {
-  const uint64_t addr = smem_u32(tile);
-  uint64_t d = (addr >> 4) & 0x3FFFull;
-  d |= 1ull << 16;                   // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
-  d |= 1ull << 46;                   // version
-  d |= 2ull << 61;                   // SWIZZLE_128B
-  return d;
-}
-
-// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, M = 128, N = n.
-__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
-         ((uint32_t)(kTcBM >> 4) << 24);
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
-                                            uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
-      "{%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
-                                          uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(da), "l"(db), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void umma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                   smem_u32(bar))
-               : "memory");
-}
-
-template <int NCOL>
-__device__ __forceinline__ void tmem_load_32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
-      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_load_16(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
+using tc::fence_after_sync;
+using tc::fence_before_sync;
+using tc::idesc_bf16;
+using tc::smem_desc_sw128;
+using tc::tma_load_2d;
+using tc::tmem_load_16;
+using tc::tmem_load_32;
+using tc::umma_bf16;
+using tc::umma_commit;
+using tc::wait_bounded;
+constexpr int kTcBM = tc::kBM, kTcBK = tc::kBK;
 
 }  // namespace
 
@@ -190,7 +118,7 @@ __global__ void __launch_bounds__(128) k_gemm_tn_tc(const __grid_constant__ CUte
     for (int c0 = 0; c0 < BN; c0 += 32) {
       float v[32];
       if (BN >= 32)
-        tmem_load_32<32>(lane_base + (uint32_t)c0, v);
+        tmem_load_32(lane_base + (uint32_t)c0, v);
       else
         tmem_load_16(lane_base + (uint32_t)c0, v);
       if (row < M) {
@@ -220,34 +148,6 @@ __global__ void __launch_bounds__(128) k_gemm_tn_tc(const __grid_constant__ CUte
 // ---------------------------------------------------------------- host side
 namespace {
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
-  return fn;
-}
-
-// 2-D map of a row-major BF16 matrix (rows x cols, leading dimension ld),
-// boxes of box_rows x 64 with 128-byte swizzle.
-bool make_map(CUtensorMap *map, const __nv_bfloat16 *ptr, int rows, int cols, int ld,
-              int box_rows) {
-  auto fn = encode_fn();
-  if (!fn) return false;
-  cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  cuuint64_t gstride[1] = {(cuuint64_t)ld * 2};
-  cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
-  cuuint32_t estride[2] = {1, 1};
-  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(ptr), gdim,
-            gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 // Dynamic shared memory per CTA.  For BN = 128 it is padded to 56 KB so at
 // most 4 CTAs share an SM: 4 x 128 tensor-memory columns = the SM's 512, so
 // no tcgen05.alloc has to wait for another CTA to free its columns.
@@ -271,7 +171,7 @@ cudaError_t launch_gemm_tn_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat
   splits = (K + kps - 1) / kps;
   if (splits > 1) mode = kGemmAtomic;
   CUtensorMap ta, tb;
-  if (!make_map(&ta, A, M, K, lda, kTcBM) || !make_map(&tb, B, N, K, ldb, N))
+  if (!tc::make_map_bf16(&ta, A, M, K, lda, kTcBM) || !tc::make_map_bf16(&tb, B, N, K, ldb, N))
     return cudaErrorInvalidValue;
   dim3 grid(1, (M + kTcBM - 1) / kTcBM, splits);
   if (N == 128) {
@@ -290,4 +190,33 @@ cudaError_t launch_gemm_tn_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat
   return cudaGetLastError();
 }
 
+namespace tc {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+bool make_map_bf16(CUtensorMap *map, const __nv_bfloat16 *ptr, int rows, int cols, int ld,
+                   int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  cuuint32_t estride[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(ptr), gdim,
+            gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace tc
 }  // namespace aco

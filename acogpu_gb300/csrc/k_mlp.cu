@@ -382,37 +382,6 @@ cudaError_t launch_transpose_feats(const __nv_bfloat16 *X, int E, __nv_bfloat16 
   return cudaGetLastError();
 }
 
-// Adam step on FP32 master weights, then the BF16 copies used by the GEMMs
-// (row-major and, for W2, transposed).
-__global__ void k_adam(float *__restrict__ w, float *__restrict__ g, float *__restrict__ m1,
-                       float *__restrict__ m2, int count, float lr, float b1, float b2,
-                       float eps, float bc1, float bc2, __nv_bfloat16 *__restrict__ wb,
-                       __nv_bfloat16 *__restrict__ wbt, int rows, int cols, int ldb) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
-    const float gv = g[t];
-    const float a = b1 * m1[t] + (1.0f - b1) * gv;
-    const float b = b2 * m2[t] + (1.0f - b2) * gv * gv;
-    m1[t] = a;
-    m2[t] = b;
-    const float v = w[t] - lr * (a / bc1) / (sqrtf(b / bc2) + eps);
-    w[t] = v;
-    g[t] = 0.0f;
-    if (wb) {
-      const int r = t / cols, cc = t % cols;
-      wb[(size_t)r * ldb + cc] = __float2bfloat16_rn(v);
-      if (wbt) wbt[(size_t)cc * rows + r] = __float2bfloat16_rn(v);
-    }
-  }
-}
-
-cudaError_t launch_adam(float *w, float *g, float *m1, float *m2, int count, float lr, float b1,
-                        float b2, float eps, float bc1, float bc2, __nv_bfloat16 *wb,
-                        __nv_bfloat16 *wbt, int rows, int cols, int ldb, cudaStream_t s) {
-  k_adam<<<(count + 255) / 256, 256, 0, s>>>(w, g, m1, m2, count, lr, b1, b2, eps, bc1, bc2, wb,
-                                             wbt, rows, cols, ldb);
-  return cudaGetLastError();
-}
-
 // Candidate heuristic with the prior: eta_nn = eta(gathered) * (floor + p).
 __global__ void k_apply_prior(ColonyDev c, const float *__restrict__ prob, float floor_) {
   const int64_t total = (int64_t)c.n * c.ldk;

@@ -1,0 +1,518 @@
+// k_mlp_fused.cu -- the edge-scoring MLP (12 -> 128 -> 128 -> 1, ReLU,
+// weighted logistic loss) as ONE tcgen05 kernel per pass over a set of
+// edges: forward, loss and backward of each 128-edge tile stay on the SM.
+//
+// A CTA (16 warps) owns tiles blockIdx.x, blockIdx.x + gridDim.x, ...; warp w
+// reads accumulator lanes 32(w % 4).. (the tile's rows) and columns
+// 32(w / 4).. of every 128-column accumulator.  Per tile:
+//   Z1  = X W1^T            (TMEM cols [0,128), K = 16)
+//   H1  = bf16(relu(Z1 + b1)) -> shared memory, row-major and transposed
+//   Z2  = H1 W2^T           (TMEM cols [0,128), K = 128)
+//   H2  = bf16(relu(Z2 + b2)); z = H2 . w3 + b3; p = sigmoid(z)
+//   dz  = w (p - y) / norm; dZ2 = bf16(dz w3 [H2 > 0]) -> shared, both ways
+//   dH1 = dZ2 W2            (TMEM cols [0,128))
+//   dW2 += dZ2^T H1         (TMEM cols [128,256), accumulated over tiles)
+//   dZ1 = bf16(dH1 [H1 > 0]) -> shared, transposed
+//   dW1 += dZ1^T X          (TMEM cols [256,272), accumulated over tiles)
+// The bias and w3 gradients are column sums over the rows, reduced across
+// each warp's 32 rows by a shuffle reduce-scatter and kept per lane.  At the
+// end every CTA writes its partial gradient (and loss) to its own row of
+// `part`; k_mlp_reduce sums the rows in a fixed order (deterministic, no
+// atomics) and applies the Adam step, refreshing the BF16 weight copies.
+// The BF16 rounding points are those of the layered kernels in k_mlp.cu.
+//
+// Operands come from TMA (X tile, W1, W2, W2^T; 128-byte swizzle) or are
+// written by the epilogue threads in the same swizzled K-major layout,
+// followed by fence.proxy.async before the MMA that reads them.  Thread 0
+// issues every MMA; completion is tracked by tcgen05.commit on an mbarrier.
+// Every wait is bounded; a timeout sets the error word, every thread leaves
+// the tile loop together (__syncthreads_and), in-flight copies and MMAs are
+// drained (bounded) and the tensor memory is released.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include "aco_mlp.h"
+#include "aco_tc.cuh"
+
+namespace aco {
+
+namespace {
+
+using tc::fence_after_sync;
+using tc::fence_before_sync;
+using tc::idesc_bf16;
+using tc::smem_desc_sw128;
+using tc::sw128_offset;
+using tc::tma_load_2d;
+using tc::umma_bf16;
+using tc::umma_commit;
+using tc::wait_bounded;
+
+constexpr int kThreadsF = 512;
+constexpr uint32_t kKT = 128 * 128;  // one 128-row K-tile of BF16 (16 KB)
+constexpr uint32_t kKT16 = 16 * 128;  // one 16-row K-tile (2 KB)
+// Shared-memory map (offsets from a 1024-byte aligned base).
+constexpr uint32_t oX = 0;             // X tile [128 e][64] (features 16..63 zero)
+constexpr uint32_t oW1 = 16 * 1024;    // W1 [128 o][64] (inputs 16..63 zero)
+constexpr uint32_t oW2 = 32 * 1024;    // W2 [128 o][128 i], two K-tiles
+constexpr uint32_t oA = 64 * 1024;     // H1 [e][i] -> dZ2 [e][o] -> dZ1^T [o][e]
+constexpr uint32_t oV = 96 * 1024;     // vectors, partial sums, barriers (10 KB)
+constexpr uint32_t oW2t = 106 * 1024;  // W2^T [128 i][128 o]          (training)
+constexpr uint32_t oB = 138 * 1024;    // H1^T [i][e]                  (training)
+constexpr uint32_t oC = 170 * 1024;    // dZ2^T [o][e]                 (training)
+constexpr uint32_t oXT = 202 * 1024;   // X^T [16 f][128 e], two K-tiles (training)
+constexpr uint32_t kEndTrain = 206 * 1024, kEndFwd = 106 * 1024;
+
+template <bool TRAIN>
+constexpr size_t fused_smem() {
+  return (TRAIN ? kEndTrain : kEndFwd) + 1024;
+}
+
+__device__ __forceinline__ uint32_t bf2_bits(float lo, float hi) {
+  const __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+  uint32_t u;
+  memcpy(&u, &b, 4);
+  return u;
+}
+
+__device__ __forceinline__ void st16(unsigned char *p, uint32_t v) {
+  *reinterpret_cast<unsigned short *>(p) = (unsigned short)v;
+}
+
+// Column sums over the warp's 32 rows: lane l returns the sum of a[l] over
+// the lanes (reduce-scatter, 31 shuffles; fixed order).  Destroys a.
+__device__ __forceinline__ float colsum32(float (&a)[32], int lane) {
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool up = (lane & s) != 0;
+#pragma unroll
+    for (int k = 0; k < s; k++) {
+      const float send = up ? a[k] : a[k + s];
+      const float keep = up ? a[k + s] : a[k];
+      a[k] = keep + __shfl_xor_sync(kFull, send, s);
+    }
+  }
+  return a[0];
+}
+
+// 32 BF16 values (packed pairs) as row `r` of a K-major operand, columns
+// c0..c0+31 (c0 a multiple of 32): four 16-byte stores.
+__device__ __forceinline__ void store_row32(unsigned char *op, int r, int c0,
+                                            const uint32_t (&pk)[16]) {
+  unsigned char *t = op + (c0 >> 6) * kKT;
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+    *reinterpret_cast<uint4 *>(t + sw128_offset(r, (c0 & 63) + 8 * u)) =
+        make_uint4(pk[4 * u], pk[4 * u + 1], pk[4 * u + 2], pk[4 * u + 3]);
+}
+
+// The same 32 values as column `r` (K index) of rows c0..c0+31 of a
+// K-major operand with 128 rows: 32 two-byte stores.
+__device__ __forceinline__ void store_col32(unsigned char *op, int r, int c0,
+                                            const uint32_t (&pk)[16]) {
+  unsigned char *t = op + (r >> 6) * kKT;
+#pragma unroll
+  for (int j = 0; j < 32; j++)
+    st16(t + sw128_offset(c0 + j, r & 63), (j & 1) ? pk[j >> 1] >> 16 : pk[j >> 1]);
+}
+
+// MMAs of a 128 x N product with K = 128 (two K-tiles): A K-tiles kKT
+// apart, B K-tiles b_step apart.
+__device__ __forceinline__ void mma_k128(uint32_t d, const unsigned char *a, const unsigned char *b,
+                                         uint32_t b_step, uint32_t idesc, bool accumulate) {
+#pragma unroll
+  for (int kt = 0; kt < 2; kt++) {
+    const uint64_t da = smem_desc_sw128(a + kt * kKT), db = smem_desc_sw128(b + kt * b_step);
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      umma_bf16(d, da + 2 * j, db + 2 * j, idesc, (accumulate || kt || j) ? 1u : 0u);
+  }
+}
+
+}  // namespace
+
+template <bool TRAIN>
+__global__ void __launch_bounds__(kThreadsF, 1)
+    k_mlp_fused(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW1,
+                const __grid_constant__ CUtensorMap tmW2, const __grid_constant__ CUtensorMap tmW2t,
+                const float *__restrict__ w, const float *__restrict__ labels, int rows,
+                float pos_weight, float norm, float *__restrict__ out, float *__restrict__ part,
+                int part_ld, uint32_t *err) {
+  extern __shared__ __align__(1024) unsigned char smem_f[];
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_f) + 1023) & ~uintptr_t(1023));
+  unsigned char *sX = base + oX, *sW1 = base + oW1, *sW2 = base + oW2, *sA = base + oA;
+  unsigned char *sW2t = base + oW2t, *sB = base + oB, *sC = base + oC, *sXT = base + oXT;
+  float *b1s = reinterpret_cast<float *>(base + oV);
+  float *b2s = b1s + 128, *w3s = b2s + 128;
+  float *zpart = w3s + 128;    // [4 column blocks][128 rows]
+  float *colsum = zpart + 512;  // [3 sums][4 lane quadrants][128 columns]
+  float *red = colsum + 1536;   // [8]
+  uint64_t *bar_x = reinterpret_cast<uint64_t *>(red + 8);
+  uint64_t *bar_w = bar_x + 1, *bar_mma = bar_x + 2, *bar_drain = bar_x + 3;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_x + 4);
+
+  constexpr uint32_t kCols = TRAIN ? 512 : 128;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = warp & 3, cb = warp >> 2;  // lane quadrant, column block
+  const int row = q * 32 + lane;           // this thread's row of the tile
+  const int c0 = cb * 32;                  // this thread's first column
+  const int tiles = (rows + 127) >> 7;
+
+  if (warp == 0) tc::tmem_alloc(tmem_slot, kCols);
+  if (threadIdx.x == 0) {
+    mbar_init(bar_x, 1);
+    mbar_init(bar_w, 1);
+    mbar_init(bar_mma, 1);
+    mbar_init(bar_drain, 1);
+    fence_barrier_init();
+  }
+  if (threadIdx.x < 128) {
+    b1s[threadIdx.x] = w[kParamB1 + threadIdx.x];
+    b2s[threadIdx.x] = w[kParamB2 + threadIdx.x];
+    w3s[threadIdx.x] = w[kParamW3 + threadIdx.x];
+  }
+  const float b3 = w[kParamB3];
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16);  // this warp's lane quadrant
+
+  int tile = blockIdx.x;
+  bool x_inflight = false;  // thread 0: a TMA load of X not yet waited for
+  if (threadIdx.x == 0 && tile < tiles) {
+    mbar_arrive_expect_tx(bar_w, (TRAIN ? 5u : 3u) * kKT);
+    tma_load_2d(sW1, &tmW1, 0, 0, bar_w);
+    tma_load_2d(sW2, &tmW2, 0, 0, bar_w);
+    tma_load_2d(sW2 + kKT, &tmW2, 64, 0, bar_w);
+    if (TRAIN) {
+      tma_load_2d(sW2t, &tmW2t, 0, 0, bar_w);
+      tma_load_2d(sW2t + kKT, &tmW2t, 64, 0, bar_w);
+    }
+    mbar_arrive_expect_tx(bar_x, kKT);
+    tma_load_2d(sX, &tmX, 0, tile * 128, bar_x);
+    x_inflight = true;
+  }
+
+  uint32_t ph_x = 0, ph_m = 0;
+  bool w_ready = false, failed = false;
+  float gw3a = 0.0f, gb2a = 0.0f, gb1a = 0.0f, lossa = 0.0f, gb3a = 0.0f;
+  for (int it = 0; tile < tiles; tile += gridDim.x, it++) {
+    // ---- Z1 = X W1^T (covers the previous tile's dW1 as well)
+    bool ok = wait_bounded(bar_x, ph_x, err);
+    ph_x ^= 1u;
+    if (threadIdx.x == 0) {
+      x_inflight = !ok;
+      if (ok && !w_ready) ok = w_ready = wait_bounded(bar_w, 0, err);
+      if (ok) {
+        fence_after_sync();
+        umma_bf16(tmem, smem_desc_sw128(sX), smem_desc_sw128(sW1), idesc_bf16(128), 0u);
+        umma_commit(bar_mma);
+      }
+    }
+    if (!__syncthreads_and(ok)) {
+      failed = true;
+      break;
+    }
+    ok = wait_bounded(bar_mma, ph_m, err);
+    ph_m ^= 1u;
+    fence_after_sync();
+    // ---- H1 = bf16(relu(Z1 + b1)): row-major (A of Z2), transposed (B of dW2)
+    uint32_t m1 = 0;  // [H1 > 0] of this thread's 32 columns
+    {
+      float v[32];
+      tc::tmem_load_32(tl + (uint32_t)c0, v);
+      uint32_t pk[16];
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        const uint32_t u = bf2_bits(fmaxf(v[2 * i] + b1s[c0 + 2 * i], 0.0f),
+                                    fmaxf(v[2 * i + 1] + b1s[c0 + 2 * i + 1], 0.0f));
+        pk[i] = u;
+        m1 |= ((u & 0x7FFFu) ? 1u : 0u) << (2 * i);
+        m1 |= ((u & 0x7FFF0000u) ? 1u : 0u) << (2 * i + 1);
+      }
+      store_row32(sA, row, c0, pk);
+      if (TRAIN) store_col32(sB, row, c0, pk);
+    }
+    if (TRAIN && cb == 1) {  // X^T (B of dW1) from the staged X tile
+      const unsigned char *xr = sX + row * 128;
+      const uint4 lo = *reinterpret_cast<const uint4 *>(xr + ((0 ^ (row & 7)) << 4));
+      const uint4 hi = *reinterpret_cast<const uint4 *>(xr + ((1 ^ (row & 7)) << 4));
+      const uint32_t f[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+      unsigned char *t = sXT + (row >> 6) * kKT16;
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        st16(t + sw128_offset(j, row & 63), (j & 1) ? f[j >> 1] >> 16 : f[j >> 1]);
+    }
+    fence_proxy_async();
+    fence_before_sync();
+    if (!__syncthreads_and(ok)) {
+      failed = true;
+      break;
+    }
+    // ---- Z2 = H1 W2^T; then prefetch the next X tile (sX is free)
+    if (threadIdx.x == 0) {
+      fence_after_sync();
+      mma_k128(tmem, sA, sW2, kKT, idesc_bf16(128), false);
+      umma_commit(bar_mma);
+      if (tile + (int)gridDim.x < tiles) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar_x, kKT);
+        tma_load_2d(sX, &tmX, 0, (tile + gridDim.x) * 128, bar_x);
+        x_inflight = true;
+      }
+    }
+    ok = wait_bounded(bar_mma, ph_m, err);
+    ph_m ^= 1u;
+    fence_after_sync();
+    // ---- H2 = bf16(relu(Z2 + b2)); z = H2 . w3 + b3
+    float h[32];
+    uint32_t m2 = 0;
+    {
+      float v[32];
+      tc::tmem_load_32(tl + (uint32_t)c0, v);
+      float zp = 0.0f;
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        h[i] = __bfloat162float(__float2bfloat16_rn(fmaxf(v[i] + b2s[c0 + i], 0.0f)));
+        m2 |= (h[i] > 0.0f ? 1u : 0u) << i;
+        zp = fmaf(h[i], w3s[c0 + i], zp);
+      }
+      zpart[cb * 128 + row] = zp;
+    }
+    fence_before_sync();
+    __syncthreads();
+    const float z = (((zpart[row] + zpart[128 + row]) + zpart[256 + row]) + zpart[384 + row]) + b3;
+    const float p = 1.0f / (1.0f + __expf(-z));
+    const int grow = tile * 128 + row;
+    if (!TRAIN) {
+      if (cb == 0 && grow < rows) out[grow] = p;
+      if (!__syncthreads_and(ok)) {
+        failed = true;
+        break;
+      }
+      continue;
+    }
+    // ---- loss, dz; w3 and b3 gradients; dZ2 (A of dH1, and transposed A of dW2)
+    const float yv = grow < rows ? labels[grow] : -1.0f;
+    float dz = 0.0f;
+    if (yv >= 0.0f) {  // rows past the set and padding rows (label -1) add nothing
+      const float wt = yv > 0.5f ? pos_weight : 1.0f;
+      dz = wt * (p - yv) / norm;
+      if (cb == 0) {
+        lossa += wt * (fmaxf(z, 0.0f) - z * yv + log1pf(__expf(-fabsf(z)))) / norm;
+        gb3a += dz;
+      }
+    }
+    {
+      float d[32];
+      uint32_t pk[16];
+#pragma unroll
+      for (int i = 0; i < 32; i++) d[i] = ((m2 >> i) & 1u) ? dz * w3s[c0 + i] : 0.0f;
+#pragma unroll
+      for (int i = 0; i < 16; i++) pk[i] = bf2_bits(d[2 * i], d[2 * i + 1]);
+      store_row32(sA, row, c0, pk);
+      store_col32(sC, row, c0, pk);
+      gb2a += colsum32(d, lane);
+#pragma unroll
+      for (int i = 0; i < 32; i++) h[i] *= dz;
+      gw3a += colsum32(h, lane);
+    }
+    fence_proxy_async();
+    fence_before_sync();
+    if (!__syncthreads_and(ok)) {
+      failed = true;
+      break;
+    }
+    // ---- dH1 = dZ2 W2 (B rows: W2^T); dW2 += dZ2^T H1
+    if (threadIdx.x == 0) {
+      fence_after_sync();
+      mma_k128(tmem, sA, sW2t, kKT, idesc_bf16(128), false);
+      mma_k128(tmem + 128, sC, sB, kKT, idesc_bf16(128), it > 0);
+      umma_commit(bar_mma);
+    }
+    ok = wait_bounded(bar_mma, ph_m, err);
+    ph_m ^= 1u;
+    fence_after_sync();
+    // ---- dZ1 = dH1 [H1 > 0] -> transposed (A of dW1); b1 gradient
+    {
+      float v[32];
+      tc::tmem_load_32(tl + (uint32_t)c0, v);
+      uint32_t pk[16];
+#pragma unroll
+      for (int i = 0; i < 32; i++) v[i] = ((m1 >> i) & 1u) ? v[i] : 0.0f;
+#pragma unroll
+      for (int i = 0; i < 16; i++) pk[i] = bf2_bits(v[2 * i], v[2 * i + 1]);
+      store_col32(sA, row, c0, pk);
+      gb1a += colsum32(v, lane);
+    }
+    fence_proxy_async();
+    fence_before_sync();
+    if (!__syncthreads_and(ok)) {
+      failed = true;
+      break;
+    }
+    // ---- dW1 += dZ1^T X (committed with the next tile's Z1, or the drain)
+    if (threadIdx.x == 0) {
+      fence_after_sync();
+      mma_k128(tmem + 256, sA, sXT, kKT16, idesc_bf16(16), it > 0);
+    }
+  }
+
+  // Drain: every MMA issued so far, and a prefetch never waited for.
+  if (threadIdx.x == 0) {
+    umma_commit(bar_drain);
+    if (x_inflight) wait_bounded(bar_x, ph_x, err);
+  }
+  const bool drained = wait_bounded(bar_drain, 0, err);
+  fence_after_sync();
+  const bool good = __syncthreads_and(drained && !failed);
+  if (TRAIN && good && (int)blockIdx.x < tiles) {
+    float *pr = part + (size_t)blockIdx.x * part_ld;
+    {
+      float v[32];  // dW2 rows o = row, columns i = c0..c0+31
+      tc::tmem_load_32(tl + 128u + (uint32_t)c0, v);
+      float4 *dst = reinterpret_cast<float4 *>(pr + kParamW2 + row * kHidden + c0);
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        dst[u] = make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+    }
+    if (cb == 0) {
+      float v[32];  // dW1 row o = row, features 0..15 (12 real)
+      tc::tmem_load_16(tl + 256u, v);
+#pragma unroll
+      for (int f = 0; f < kFeatures; f++) pr[kParamW1 + row * kFeatures + f] = v[f];
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        lossa += __shfl_xor_sync(kFull, lossa, o);
+        gb3a += __shfl_xor_sync(kFull, gb3a, o);
+      }
+      if (lane == 0) {
+        red[q] = lossa;
+        red[4 + q] = gb3a;
+      }
+    }
+    colsum[(0 * 4 + q) * 128 + c0 + lane] = gw3a;
+    colsum[(1 * 4 + q) * 128 + c0 + lane] = gb2a;
+    colsum[(2 * 4 + q) * 128 + c0 + lane] = gb1a;
+    __syncthreads();
+    if (threadIdx.x < 128) {
+      const int t = threadIdx.x;
+      const float *s0 = colsum, *s1 = colsum + 512, *s2 = colsum + 1024;
+      pr[kParamW3 + t] = ((s0[t] + s0[128 + t]) + s0[256 + t]) + s0[384 + t];
+      pr[kParamB2 + t] = ((s1[t] + s1[128 + t]) + s1[256 + t]) + s1[384 + t];
+      pr[kParamB1 + t] = ((s2[t] + s2[128 + t]) + s2[256 + t]) + s2[384 + t];
+    }
+    if (threadIdx.x == 0) {
+      pr[kParamB3] = ((red[4] + red[5]) + red[6]) + red[7];
+      pr[kParamCount] = ((red[0] + red[1]) + red[2]) + red[3];
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+}
+
+// Sums the per-CTA partial rows (columns 0..kParamCount; the last is the
+// loss) in CTA order and, with `adam`, applies the Adam step to the FP32
+// masters and refreshes their BF16 copies: W1 into its 16-wide padded rows,
+// W2 row-major and transposed.  `clear` zeroes the rows read (one row only).
+__global__ void __launch_bounds__(256)
+    k_mlp_reduce(float *__restrict__ part, int G, int ld, int clear, float *__restrict__ gout,
+                 float *__restrict__ loss_out, int adam, float *__restrict__ w,
+                 float *__restrict__ m1, float *__restrict__ m2, float lr, float b1, float b2,
+                 float eps, float bc1, float bc2, __nv_bfloat16 *__restrict__ w1b,
+                 __nv_bfloat16 *__restrict__ w2b, __nv_bfloat16 *__restrict__ w2tb) {
+  __shared__ float sh[8][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int t = blockIdx.x * 32 + tx;
+  const bool live = t < kParamCount || (t == kParamCount && loss_out);
+  float s = 0.0f;
+  if (live)
+    for (int c = ty; c < G; c += 8) s += part[(size_t)c * ld + t];
+  sh[ty][tx] = s;
+  __syncthreads();
+  if (ty != 0 || !live) return;
+  s = sh[0][tx];
+#pragma unroll
+  for (int y = 1; y < 8; y++) s += sh[y][tx];
+  if (clear) part[t] = 0.0f;
+  if (t == kParamCount) {
+    *loss_out = s;
+    return;
+  }
+  if (gout) gout[t] = s;
+  if (!adam) return;
+  const float a = b1 * m1[t] + (1.0f - b1) * s;
+  const float b = b2 * m2[t] + (1.0f - b2) * s * s;
+  m1[t] = a;
+  m2[t] = b;
+  const float v = w[t] - lr * (a / bc1) / (sqrtf(b / bc2) + eps);
+  w[t] = v;
+  const __nv_bfloat16 vb = __float2bfloat16_rn(v);
+  if (t < kParamB1) {
+    w1b[(t / kFeatures) * kFeatPad + t % kFeatures] = vb;
+  } else if (t >= kParamW2 && t < kParamB2) {
+    const int o = (t - kParamW2) / kHidden, i = (t - kParamW2) % kHidden;
+    w2b[o * kHidden + i] = vb;
+    w2tb[i * kHidden + o] = vb;
+  }
+}
+
+int mlp_fused_grid(int rows, int sms) {
+  const int tiles = (rows + 127) / 128;
+  return tiles < sms ? tiles : sms;
+}
+
+cudaError_t launch_mlp_fused(bool train, const __nv_bfloat16 *X, int rows,
+                             const __nv_bfloat16 *w1b, const __nv_bfloat16 *w2b,
+                             const __nv_bfloat16 *w2tb, const float *w, const float *labels,
+                             float pos_weight, float norm, float *out, float *part, int part_ld,
+                             int grid, uint32_t *err, cudaStream_t s) {
+  if (rows < 1 || grid < 1 || grid > (rows + 127) / 128) return cudaErrorInvalidValue;
+  if ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(w1b) |
+       reinterpret_cast<uintptr_t>(w2b) | reinterpret_cast<uintptr_t>(w2tb) |
+       reinterpret_cast<uintptr_t>(part)) & 15)
+    return cudaErrorInvalidValue;
+  if (train && (part_ld & 3)) return cudaErrorInvalidValue;
+  CUtensorMap tx, t1, t2, t2t;
+  if (!tc::make_map_bf16(&tx, X, rows, kFeatPad, kFeatPad, 128) ||
+      !tc::make_map_bf16(&t1, w1b, kHidden, kFeatPad, kFeatPad, 128) ||
+      !tc::make_map_bf16(&t2, w2b, kHidden, kHidden, kHidden, 128) ||
+      !tc::make_map_bf16(&t2t, w2tb, kHidden, kHidden, kHidden, 128))
+    return cudaErrorInvalidValue;
+  static bool configured = false;  // above the 48 KB default
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_fused<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)fused_smem<true>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_mlp_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)fused_smem<false>());
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  if (train)
+    k_mlp_fused<true><<<grid, kThreadsF, fused_smem<true>(), s>>>(
+        tx, t1, t2, t2t, w, labels, rows, pos_weight, norm, out, part, part_ld, err);
+  else
+    k_mlp_fused<false><<<grid, kThreadsF, fused_smem<false>(), s>>>(
+        tx, t1, t2, t2t, w, labels, rows, pos_weight, norm, out, part, part_ld, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_reduce(float *part, int G, int ld, bool clear, float *gout, float *loss_out,
+                              bool adam, float *w, float *m1, float *m2, float lr, float b1,
+                              float b2, float eps, float bc1, float bc2, __nv_bfloat16 *w1b,
+                              __nv_bfloat16 *w2b, __nv_bfloat16 *w2tb, cudaStream_t s) {
+  if (G < 1 || (clear && G != 1)) return cudaErrorInvalidValue;
+  const int blocks = (kParamCount + 1 + 31) / 32;
+  k_mlp_reduce<<<blocks, 256, 0, s>>>(part, G, ld, clear ? 1 : 0, gout, loss_out, adam ? 1 : 0,
+                                       w, m1, m2, lr, b1, b2, eps, bc1, bc2, w1b, w2b, w2tb);
+  return cudaGetLastError();
+}
+
+}  // namespace aco

@@ -42,8 +42,18 @@ struct aco_prior {
   __nv_bfloat16 *dZ1t = nullptr, *Xt = nullptr;        // 128 x B, 16 x B
   float *dlogit = nullptr, *out = nullptr, *loss = nullptr, *scratch = nullptr;
   float *gW1full = nullptr;  // [128][16] gradient of the padded first layer
+  // fused engine: one partial-gradient row per CTA (gradient, then loss)
+  float *part = nullptr;
+  int part_rows = 0;
+  float *slots = nullptr;  // per-batch losses of the current epoch
+  int64_t slots_cap = 0;
+  int sms = 0;
+  // features and probabilities of the colony being scored (aco_prior_apply)
+  __nv_bfloat16 *ax = nullptr;
+  float *aprob = nullptr;
+  int64_t a_cap = 0;
   int64_t step = 0;
-  int engine = ACO_GEMM_TCGEN05;  // enum aco_gemm_engine
+  int engine = ACO_GEMM_FUSED;  // enum aco_gemm_engine
   std::string err;
 };
 
@@ -145,7 +155,7 @@ int ensure_workspace(aco_prior *p, int B) {
 // Forward pass over rows X[0..B) (B a multiple of 128); with labels also the
 // loss and the gradients, accumulated into p->g (W1 part via gW1full).
 int forward_backward(aco_prior *p, const __nv_bfloat16 *X, const float *Y, int B, int valid,
-                     float pos_weight, bool backward, float *probs_dev) {
+                     float pos_weight, bool backward, float *probs_dev, float *loss_dev) {
   cudaStream_t s = p->stream;
   const int splits = std::max(1, std::min(64, B / 1024));
   // Z1 = X W1^T ; H1 = relu(Z1 + b1)
@@ -164,7 +174,7 @@ int forward_backward(aco_prior *p, const __nv_bfloat16 *X, const float *Y, int B
   }
   ACO_PCUDA(p, launch_head(p->H2, p->w + kParamW3, p->w + kParamB3, B, Y, pos_weight,
                            (float)std::max(1, valid), nullptr, p->dlogit, p->g + kParamW3,
-                           p->g + kParamB3, p->loss, s), "head");
+                           p->g + kParamB3, loss_dev, s), "head");
   // dZ2 = dlogit w3 * [H2 > 0]
   ACO_PCUDA(p, launch_grad_hidden2(p->dlogit, p->w + kParamW3, p->H2, B, p->dZ2, p->dZ2t, B,
                                    p->g + kParamB2, s), "dz2");
@@ -199,13 +209,64 @@ int pack_grads(aco_prior *p) {
   return ACO_OK;
 }
 
-int adam_step(aco_prior *p, float lr) {
+// Row pitch of the fused engine's partial-gradient rows (gradient + loss).
+constexpr int kPartLd = (kParamCount + 1 + 3) / 4 * 4;
+
+int ensure_fused(aco_prior *p, int rows) {
+  if (!p->sms) {
+    int dev = 0;
+    ACO_PCUDA(p, cudaGetDevice(&dev), "device");
+    ACO_PCUDA(p, cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev), "SMs");
+  }
+  const int G = mlp_fused_grid(rows, p->sms);
+  if (G > p->part_rows) {
+    cudaFree(p->part);
+    p->part = nullptr;
+    p->part_rows = 0;
+    ACO_PCUDA(p, alloc(&p->part, (size_t)G * kPartLd), "alloc partials");
+    p->part_rows = G;
+  }
+  return ACO_OK;
+}
+
+int ensure_slots(aco_prior *p, int64_t n) {
+  if (n <= p->slots_cap) return ACO_OK;
+  cudaFree(p->slots);
+  p->slots = nullptr;
+  p->slots_cap = 0;
+  ACO_PCUDA(p, alloc(&p->slots, (size_t)n), "alloc loss slots");
+  p->slots_cap = n;
+  return ACO_OK;
+}
+
+// One Adam step from the summed gradient rows (the fused engine's
+// partials, or the layered engines' accumulated vector, which is cleared),
+// with the BF16 weight copies refreshed on the device: no host round trip.
+int adam_step(aco_prior *p, float lr, float *part, int G, int ld, bool clear, float *loss_out) {
   p->step++;
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   const float bc1 = 1.0f - powf(b1, (float)p->step), bc2 = 1.0f - powf(b2, (float)p->step);
-  ACO_PCUDA(p, launch_adam(p->w, p->g, p->m1, p->m2, kParamCount, lr, b1, b2, eps, bc1, bc2,
-                           nullptr, nullptr, 0, 0, 0, p->stream), "adam");
-  return sync_bf16(p);
+  ACO_PCUDA(p, launch_mlp_reduce(part, G, ld, clear, nullptr, loss_out, true, p->w, p->m1, p->m2,
+                                 lr, b1, b2, eps, bc1, bc2, p->w1b, p->w2b, p->w2tb, p->stream),
+            "adam");
+  return ACO_OK;
+}
+
+// Forward (+ backward) of rows X[0..rows) on the fused engine; with labels
+// the summed gradient goes to gout and the loss to loss_out.
+int fused_pass(aco_prior *p, const __nv_bfloat16 *X, const float *Y, int rows, float pos_weight,
+               float *probs, float *gout, float *loss_out) {
+  if (int s = ensure_fused(p, rows)) return s;
+  const int G = mlp_fused_grid(rows, p->sms);
+  uint32_t *err = reinterpret_cast<uint32_t *>(p->scratch + 2);
+  ACO_PCUDA(p, launch_mlp_fused(Y != nullptr, X, rows, p->w1b, p->w2b, p->w2tb, p->w, Y,
+                                pos_weight, (float)std::max(1, rows), probs, p->part, kPartLd, G,
+                                err, p->stream), "fused mlp");
+  if (Y)
+    ACO_PCUDA(p, launch_mlp_reduce(p->part, G, kPartLd, false, gout, loss_out, false, p->w,
+                                   p->m1, p->m2, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 1.0f, nullptr,
+                                   nullptr, nullptr, p->stream), "reduce");
+  return ACO_OK;
 }
 
 // Uploads host examples (E x 12 FP32 features) into padded BF16 rows.
@@ -345,16 +406,18 @@ int aco_prior_train(aco_prior *p, int32_t epochs, int32_t batch, float lr, uint6
   if (!p || epochs < 0 || batch < 128) return ACO_ERR_INVALID_ARGUMENT;
   if (p->E == 0) return pfail(p, ACO_ERR_NOT_INITIALIZED, "no training examples");
   const int B = round_rows(batch);
-  if (int s = ensure_workspace(p, B)) return s;
+  const bool fused = p->engine == ACO_GEMM_FUSED;
+  if (int s = fused ? ensure_fused(p, B) : ensure_workspace(p, B)) return s;
   const float pos_weight =
       p->positives ? (float)(p->E - p->positives) / (float)p->positives : 1.0f;
   const int64_t nb = (p->E + B - 1) / B;
+  if (int s = ensure_slots(p, nb)) return s;
   std::vector<int64_t> order((size_t)nb);
   std::mt19937_64 rng(seed);
   __nv_bfloat16 *Xtail = nullptr;
   float *Ytail = nullptr;
   const int64_t tail = p->E - (nb - 1) * B;  // rows of the last batch
-  if (tail < B) {  // the last batch is padded with label -1 rows
+  if (tail < B && !fused) {  // the layered engines pad the last batch with label -1 rows
     ACO_PCUDA(p, alloc(&Xtail, (size_t)B * kFeatPad), "alloc");
     ACO_PCUDA(p, alloc(&Ytail, (size_t)B), "alloc");
     ACO_PCUDA(p, zero(p, Xtail, (size_t)B * kFeatPad * 2), "memset");
@@ -365,29 +428,56 @@ int aco_prior_train(aco_prior *p, int32_t epochs, int32_t batch, float lr, uint6
     ACO_PCUDA(p, copy_sync(p, Ytail, p->Y + (size_t)(nb - 1) * B, (size_t)tail * 4,
                            cudaMemcpyDeviceToDevice), "tail");
   }
-  float loss = 0.0f;
-  for (int ep = 0; ep < epochs; ep++) {
+  // No host synchronisation inside an epoch: each batch's loss lands in its
+  // own device slot, and only the last epoch's slots are read back.
+  int s = ACO_OK;
+  for (int ep = 0; ep < epochs && !s; ep++) {
     for (int64_t q = 0; q < nb; q++) order[q] = q;
     std::shuffle(order.begin(), order.end(), rng);
-    double ep_loss = 0.0;
-    for (int64_t q : order) {
-      const bool last = q == nb - 1 && Xtail;
-      const __nv_bfloat16 *X = last ? Xtail : p->X + (size_t)q * B * kFeatPad;
-      const float *Y = last ? Ytail : p->Y + (size_t)q * B;
-      const int valid = last ? (int)tail : B;
-      ACO_PCUDA(p, cudaMemsetAsync(p->loss, 0, 4, p->stream), "memset");
-      if (int s = forward_backward(p, X, Y, B, valid, pos_weight, true, nullptr)) return s;
-      if (int s = pack_grads(p)) return s;
-      if (int s = adam_step(p, lr)) return s;
-      float h = 0.0f;
-      ACO_PCUDA(p, cudaMemcpyAsync(&h, p->loss, 4, cudaMemcpyDeviceToHost, p->stream), "loss");
-      ACO_PCUDA(p, cudaStreamSynchronize(p->stream), "synchronize");
-      ep_loss += h;
+    if (!fused && cudaMemsetAsync(p->slots, 0, (size_t)nb * 4, p->stream) != cudaSuccess)
+      s = pfail(p, ACO_ERR_CUDA, "memset");
+    for (int64_t b = 0; b < nb && !s; b++) {
+      const int64_t q = order[(size_t)b];
+      const int valid = q == nb - 1 ? (int)tail : B;
+      if (fused) {
+        const __nv_bfloat16 *X = p->X + (size_t)q * B * kFeatPad;
+        const float *Y = p->Y + (size_t)q * B;
+        if (!(s = ensure_fused(p, valid))) {
+          const int G = mlp_fused_grid(valid, p->sms);
+          uint32_t *err = reinterpret_cast<uint32_t *>(p->scratch + 2);
+          if (launch_mlp_fused(true, X, valid, p->w1b, p->w2b, p->w2tb, p->w, Y, pos_weight,
+                               (float)std::max(1, valid), nullptr, p->part, kPartLd, G, err,
+                               p->stream) != cudaSuccess)
+            s = pfail(p, ACO_ERR_CUDA, "fused mlp");
+          if (!s) s = adam_step(p, lr, p->part, G, kPartLd, false, p->slots + b);
+        }
+      } else {
+        const bool last = q == nb - 1 && Xtail;
+        const __nv_bfloat16 *X = last ? Xtail : p->X + (size_t)q * B * kFeatPad;
+        const float *Y = last ? Ytail : p->Y + (size_t)q * B;
+        s = forward_backward(p, X, Y, B, valid, pos_weight, true, nullptr, p->slots + b);
+        if (!s) s = pack_grads(p);
+        if (!s) s = adam_step(p, lr, p->g, 1, kParamCount, true, nullptr);
+      }
     }
-    loss = (float)(ep_loss / nb);
   }
+  float loss = 0.0f;
+  if (!s && epochs > 0) {
+    std::vector<float> h((size_t)nb);
+    if (cudaMemcpyAsync(h.data(), p->slots, (size_t)nb * 4, cudaMemcpyDeviceToHost, p->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(p->stream) != cudaSuccess)
+      s = pfail(p, ACO_ERR_CUDA, "read losses");
+    double ep_loss = 0.0;
+    for (float v : h) ep_loss += v;
+    loss = (float)(ep_loss / nb);
+  } else if (!s) {
+    s = cudaStreamSynchronize(p->stream) == cudaSuccess ? ACO_OK : ACO_ERR_CUDA;
+  }
+  cudaStreamSynchronize(p->stream);
   cudaFree(Xtail);
   cudaFree(Ytail);
+  if (s) return s;
   if (last_loss) *last_loss = loss;
   return gemm_status(p);
 }
@@ -396,14 +486,20 @@ int aco_prior_loss_and_grads(aco_prior *p, const float *feats, const float *labe
                              float pos_weight, float *loss, float *grads) {
   if (!p || !feats || !labels || E < 1 || !grads) return ACO_ERR_INVALID_ARGUMENT;
   const int B = round_rows(E);
-  if (int s = ensure_workspace(p, B)) return s;
+  const bool fused = p->engine == ACO_GEMM_FUSED;
+  if (int s = fused ? ensure_fused(p, E) : ensure_workspace(p, B)) return s;
   __nv_bfloat16 *X = nullptr;
   float *Y = nullptr;
   if (int s = upload_examples(p, feats, labels, E, B, &X, &Y)) return s;
-  ACO_PCUDA(p, cudaMemsetAsync(p->g, 0, sizeof(float) * kParamCount, p->stream), "memset");
-  ACO_PCUDA(p, cudaMemsetAsync(p->loss, 0, 4, p->stream), "memset");
-  int s = forward_backward(p, X, Y, B, E, pos_weight, true, nullptr);
-  if (!s) s = pack_grads(p);
+  int s = ACO_OK;
+  if (fused) {
+    s = fused_pass(p, X, Y, E, pos_weight, nullptr, p->g, p->loss);
+  } else {
+    ACO_PCUDA(p, cudaMemsetAsync(p->g, 0, sizeof(float) * kParamCount, p->stream), "memset");
+    ACO_PCUDA(p, cudaMemsetAsync(p->loss, 0, 4, p->stream), "memset");
+    s = forward_backward(p, X, Y, B, E, pos_weight, true, nullptr, p->loss);
+    if (!s) s = pack_grads(p);
+  }
   float h = 0.0f;
   if (!s) {
     cudaMemcpyAsync(&h, p->loss, 4, cudaMemcpyDeviceToHost, p->stream);
@@ -411,6 +507,7 @@ int aco_prior_loss_and_grads(aco_prior *p, const float *feats, const float *labe
     if (cudaStreamSynchronize(p->stream) != cudaSuccess) s = ACO_ERR_CUDA;
     cudaMemsetAsync(p->g, 0, sizeof(float) * kParamCount, p->stream);
   }
+  cudaStreamSynchronize(p->stream);
   cudaFree(X);
   cudaFree(Y);
   if (loss) *loss = h;
@@ -420,15 +517,23 @@ int aco_prior_loss_and_grads(aco_prior *p, const float *feats, const float *labe
 int aco_prior_predict(aco_prior *p, const float *feats, int32_t E, float *probs) {
   if (!p || !feats || E < 1 || !probs) return ACO_ERR_INVALID_ARGUMENT;
   const int B = round_rows(E);
-  if (int s = ensure_workspace(p, B)) return s;
+  const bool fused = p->engine == ACO_GEMM_FUSED;
+  if (int s = fused ? ensure_fused(p, E) : ensure_workspace(p, B)) return s;
   __nv_bfloat16 *X = nullptr;
   float *Y = nullptr;
   if (int s = upload_examples(p, feats, nullptr, E, B, &X, &Y)) return s;
-  int s = forward_backward(p, X, nullptr, B, E, 1.0f, false, p->out);
-  if (!s && cudaMemcpyAsync(probs, p->out, (size_t)E * 4, cudaMemcpyDeviceToHost, p->stream) !=
+  float *out = p->out;
+  int s = ACO_OK;
+  if (fused && alloc(&out, (size_t)B) != cudaSuccess) s = ACO_ERR_OUT_OF_MEMORY;
+  if (!s)
+    s = fused ? fused_pass(p, X, nullptr, E, 1.0f, out, nullptr, nullptr)
+              : forward_backward(p, X, nullptr, B, E, 1.0f, false, out, nullptr);
+  if (!s && cudaMemcpyAsync(probs, out, (size_t)E * 4, cudaMemcpyDeviceToHost, p->stream) !=
                 cudaSuccess)
     s = ACO_ERR_CUDA;
   if (!s && cudaStreamSynchronize(p->stream) != cudaSuccess) s = ACO_ERR_CUDA;
+  cudaStreamSynchronize(p->stream);
+  if (fused) cudaFree(out);
   cudaFree(X);
   cudaFree(Y);
   return s ? s : gemm_status(p);
@@ -440,25 +545,36 @@ int aco_prior_apply(aco_prior *p, aco_colony *c, float floor_) {
                                               "colony must be initialized and built from coordinates");
   const int E = c->n * c->K;
   const int B = round_rows(E);
-  if (int s = ensure_workspace(p, B)) return s;
-  __nv_bfloat16 *X = nullptr;
-  float *prob = nullptr;
-  ACO_PCUDA(p, alloc(&X, (size_t)B * kFeatPad), "alloc");
-  ACO_PCUDA(p, alloc(&prob, (size_t)B), "alloc");
-  ACO_PCUDA(p, cudaMemsetAsync(X, 0, (size_t)B * kFeatPad * 2, p->stream), "memset");
+  const bool fused = p->engine == ACO_GEMM_FUSED;
+  if (int s = fused ? ensure_fused(p, E) : ensure_workspace(p, B)) return s;
+  if (B > p->a_cap) {  // kept across calls: scoring a colony allocates nothing
+    cudaFree(p->ax);
+    cudaFree(p->aprob);
+    p->ax = nullptr;
+    p->aprob = nullptr;
+    p->a_cap = 0;
+    ACO_PCUDA(p, alloc(&p->ax, (size_t)B * kFeatPad), "alloc");
+    ACO_PCUDA(p, alloc(&p->aprob, (size_t)B), "alloc");
+    p->a_cap = B;
+  }
+  __nv_bfloat16 *X = p->ax;
+  float *prob = p->aprob;
+  if (!fused && B > E)  // the layered engines read whole 128-row blocks
+    ACO_PCUDA(p, cudaMemsetAsync(X + (size_t)E * kFeatPad, 0, (size_t)(B - E) * kFeatPad * 2,
+                                 p->stream), "memset");
   ACO_PCUDA(p, cudaStreamSynchronize(c->stream), "synchronize colony");
   const ColonyDev d = colony_dev(c);
   int s = launch_edge_features(d, c->xy, c->xy + c->n, p->scratch, X, nullptr, p->stream) ==
                   cudaSuccess
               ? ACO_OK
               : ACO_ERR_CUDA;
-  if (!s) s = forward_backward(p, X, nullptr, B, E, 1.0f, false, prob);
+  if (!s)
+    s = fused ? fused_pass(p, X, nullptr, E, 1.0f, prob, nullptr, nullptr)
+              : forward_backward(p, X, nullptr, B, E, 1.0f, false, prob, nullptr);
   if (!s && launch_apply_prior(d, prob, floor_, p->stream) != cudaSuccess) s = ACO_ERR_CUDA;
   if (!s && launch_pheromone_rows(d, false, false, false, p->stream) != cudaSuccess)
     s = ACO_ERR_CUDA;
   if (!s && cudaStreamSynchronize(p->stream) != cudaSuccess) s = ACO_ERR_CUDA;
-  cudaFree(X);
-  cudaFree(prob);
   if (s) return pfail(p, s, "apply failed");
   if (int g = gemm_status(p)) return g;
   // The colony's candidate table changed: a captured iteration graph stays
@@ -496,7 +612,8 @@ int aco_colony_edge_features(aco_colony *c, float *out) {
 }
 
 int aco_prior_set_engine(aco_prior *p, int32_t engine) {
-  if (!p || (engine != ACO_GEMM_MMA_SYNC && engine != ACO_GEMM_TCGEN05))
+  if (!p || (engine != ACO_GEMM_MMA_SYNC && engine != ACO_GEMM_TCGEN05 &&
+             engine != ACO_GEMM_FUSED))
     return ACO_ERR_INVALID_ARGUMENT;
   p->engine = engine;
   return ACO_OK;
@@ -542,7 +659,7 @@ void aco_prior_destroy(aco_prior *p) {
   if (p->stream) cudaStreamSynchronize(p->stream);
   void *bufs[] = {p->w, p->g, p->m1, p->m2, p->w1b, p->w2b, p->w2tb, p->X, p->Y, p->Z, p->H1,
                   p->H1t, p->H2, p->dZ2, p->dZ2t, p->dZ1t, p->Xt, p->dlogit, p->out, p->loss,
-                  p->scratch, p->gW1full};
+                  p->scratch, p->gW1full, p->part, p->slots, p->ax, p->aprob};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);

@@ -85,8 +85,10 @@ def candidate_heuristic(colony: Colony):
 
 
 class EdgePrior:
-    """engine: ACO_GEMM_TCGEN05 (default; TMA + TMEM tensor cores) or
-    ACO_GEMM_MMA_SYNC (warp-level mma.sync) for the MLP's products."""
+    """engine: ACO_GEMM_FUSED (default: the whole forward/backward pass of
+    each 128-edge tile in one tcgen05 kernel), or the layer-by-layer
+    ACO_GEMM_TCGEN05 (TMA + TMEM tensor cores) and ACO_GEMM_MMA_SYNC
+    (warp-level mma.sync) GEMM engines."""
 
     def __init__(self, seed=0, engine=None):
         self._L = lib()

@@ -174,12 +174,12 @@ def peaks():
         return {}
 
 
-def profiled_traffic(name="construct_staged_rbas_aging_n1000.md"):
+def profiled_traffic(name="construct_staged_rbas_aging_n1000.md", key="traffic_bytes_per_launch"):
     """DRAM bytes per launch of the construction kernel, from the committed
     ncu summary (dram__bytes_read.sum + dram__bytes_write.sum of one capture)."""
     try:
         for line in open(os.path.join(ROOT, "profiles", name)):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1])
     except OSError:
         pass
@@ -669,7 +669,7 @@ def run_batch(args, rank, world, local):
     import torch
     import acogpu_gb300 as aco
     torch.cuda.set_device(local)
-    allinst = batch_instances(BATCH_COUNT * world)
+    allinst = batch_instances(args.batch_instances * world)
     sizes_all = [len(x) for x, _ in allinst]
     mine = distrib.shard_instances(sizes_all, np.minimum(sizes_all, BATCH_CAP), BATCH_K,
                                    world)[rank]
@@ -709,6 +709,11 @@ def run_batch(args, rank, world, local):
                     ((fb1 - fb0) / args.steps * 4 * my_n).sum())
     hbm = peaks().get("hbm_gbs")
     achieved = bytes_c / (tune["construct_ms"] / 1e3) / 1e9
+    # DRAM traffic: the 32-instance capture's bytes per ant-step times this
+    # shard's ant-steps (the whole batch does not fit an ncu capture).
+    t32 = profiled_traffic("construct_batch_uneven32.md")
+    s32 = profiled_traffic("construct_batch_uneven32.md", "ant_steps_per_launch")
+    batch_traffic = (t32 / s32 * float((my_m * (my_n - 1)).sum())) if (t32 and s32) else None
     best = b.glob_best()
     b.close()
     (dev_s,), (tours, launches, best_sum) = distrib.reduce_times_and_counts(
@@ -725,8 +730,9 @@ def run_batch(args, rank, world, local):
             "roofline": {"bound": "hbm", "kernel": "k_batch_construct", "achieved": achieved,
                          "peak": hbm, "unit": "GB/s", "frac": achieved / hbm if hbm else None,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm else None,
-                         "algorithmic_bytes_per_launch": bytes_c, "traffic": None,
-                         "traffic_source": "not captured: the batch holds 5+ GB on the device"},
+                         "algorithmic_bytes_per_launch": bytes_c, "traffic": batch_traffic,
+                         "traffic_source": "profiles/construct_batch_uneven32.md (ncu of one "
+                                           "launch over a 32-instance slice), scaled by ant-steps"},
             "mean_best_length": best_sum / len(allinst), "clocks": clk.summary()}
 
 
@@ -836,18 +842,24 @@ def run_learned(args, rank, world, local):
     loss0 = prior.train(epochs=1, batch=65536, lr=2e-3, seed=1)
     loss = prior.train(epochs=args.epochs, batch=65536, lr=1e-3, seed=2)
     train_s = time.perf_counter() - t0
-    # One more epoch on each GEMM engine, timed alone; the trained weights are
-    # put back afterwards so the evaluation below is unaffected.
+    # One more epoch on each engine, timed alone; the trained weights are put
+    # back afterwards so the evaluation below is unaffected.
     w_trained = prior.weights()
     epoch_s = {}
-    for name, eng in (("tcgen05", _abi.ACO_GEMM_TCGEN05), ("mma_sync", _abi.ACO_GEMM_MMA_SYNC)):
+    for name, eng in (("fused", _abi.ACO_GEMM_FUSED), ("tcgen05_layered", _abi.ACO_GEMM_TCGEN05),
+                      ("mma_sync_layered", _abi.ACO_GEMM_MMA_SYNC)):
         prior.set_engine(eng)
+        prior.train(epochs=1, batch=65536, lr=1e-6, seed=3)  # warm-up (workspace, maps)
+        torch.cuda.synchronize()
         t1 = time.perf_counter()
         prior.train(epochs=1, batch=65536, lr=1e-6, seed=3)
         epoch_s[name] = time.perf_counter() - t1
-    prior.set_engine(_abi.ACO_GEMM_TCGEN05)
+    prior.set_engine(_abi.ACO_GEMM_FUSED)
     prior.set_weights(w_trained)
-
+    # Tensor-core work of one epoch: per edge Z1 (K padded to 16), Z2, dH1,
+    # dW2 (N = 128) and dW1 (N = 16), 2 FLOP per multiply-add.
+    mlp_flop_per_edge = 2 * 128 * (16 + 128 + 128 + 128 + 16)
+    fused_tflops = mlp_flop_per_edge * examples / epoch_s["fused"] / 1e12
     sizes = instances.batch_sizes(args.eval_instances, lo=200, hi=2000, seed=41)
     evals = [instances.uniform_instance(int(n), seed=30_000 + i) if i % 2 == 0 else
              instances.clustered_instance(int(n), seed=30_000 + i) for i, n in enumerate(sizes)]
@@ -899,7 +911,11 @@ def run_learned(args, rank, world, local):
                         "reaches_plain_within_0.1pct_at_s": reach},
             "training": {"examples": examples, "positives": positives, "loss_first_epoch": loss0,
                          "loss_last_epoch": loss, "wall_s": train_s,
-                         "epoch_s_by_gemm_engine": epoch_s}}
+                         "epoch_s_by_engine": epoch_s,
+                         "tensor_flop_per_edge": mlp_flop_per_edge,
+                         "fused_epoch_tflops": fused_tflops,
+                         "fused_epoch_frac_of_measured_bf16": fused_tflops /
+                         peaks().get("bf16_tflops", 1900.0)}}
 
 
 def main():
@@ -913,6 +929,8 @@ def main():
     ap.add_argument("--workload", default="parity_batch8",
                     choices=("parity_batch8", "rbas_aging_n1000", "batch512", "learned",
                              "large4096"))
+    ap.add_argument("--batch-instances", type=int, default=BATCH_COUNT,
+                    help="instances of the uneven batch per GPU (batch512)")
     ap.add_argument("--train-instances", type=int, default=1024)
     ap.add_argument("--train-iters", type=int, default=200)
     ap.add_argument("--eval-instances", type=int, default=256)

@@ -346,16 +346,21 @@ ACO_API void aco_batch_destroy(aco_batch *b);
  * (dK = distance to the K-th candidate, d1 = to the nearest).
  * Parameters are packed as W1[128][12] b1[128] W2[128][128] b2[128] w3[128] b3. */
 typedef struct aco_prior aco_prior;
-/* Tensor-core engine of the MLP's GEMMs. */
+/* Engine of the MLP's forward and backward passes.  The first two run
+ * layer by layer (one GEMM launch per product, elementwise kernels between
+ * them); ACO_GEMM_FUSED (the default) runs the whole pass over each
+ * 128-edge tile in one tcgen05 kernel, activations kept in shared and
+ * tensor memory, gradients summed per CTA and reduced in a fixed order. */
 enum aco_gemm_engine {
-  ACO_GEMM_MMA_SYNC = 0, /* warp-level mma.sync.m16n8k16 */
-  ACO_GEMM_TCGEN05 = 1   /* tcgen05.mma with TMA-staged operands, TMEM accumulator */
+  ACO_GEMM_MMA_SYNC = 0, /* layered, warp-level mma.sync.m16n8k16 */
+  ACO_GEMM_TCGEN05 = 1,  /* layered, tcgen05.mma with TMA-staged operands, TMEM accumulator */
+  ACO_GEMM_FUSED = 2     /* one fused tcgen05 kernel per pass (default) */
 };
 ACO_API int aco_prior_create(uint64_t seed, aco_prior **out);
 ACO_API int aco_prior_set_engine(aco_prior *p, int32_t engine);
 /* The MLP's GEMM on host data, for checking: C (M x N, FP32) = A (M x K) *
  * B (N x K)^T with A and B raw BF16 bit patterns; K a multiple of 8;
- * ACO_GEMM_TCGEN05 needs N = 128 or 16. */
+ * engine ACO_GEMM_MMA_SYNC or ACO_GEMM_TCGEN05 (N = 128 or 16). */
 ACO_API int aco_gemm_bf16_tn(const uint16_t *A, const uint16_t *B, float *C, int32_t M, int32_t N,
                              int32_t K, int32_t splits, int32_t engine);
 ACO_API int aco_prior_param_count(void);

@@ -1,8 +1,11 @@
 """GPU tests of the learned heuristic prior: features, the MLP's forward and
 backward kernels against the CPU oracle, parity of a colony that uses the
 prior, and what training buys over the plain method."""
+import time
+
 import numpy as np
 import pytest
+import torch
 
 import oracle
 import acogpu_gb300 as aco
@@ -54,8 +57,9 @@ def test_edge_features_match_numpy():
     assert np.allclose(f, ref, rtol=1e-2, atol=1e-3)
 
 
-ENGINES = pytest.mark.parametrize("engine", [_abi.ACO_GEMM_TCGEN05, _abi.ACO_GEMM_MMA_SYNC],
-                                  ids=["tcgen05", "mma_sync"])
+ENGINES = pytest.mark.parametrize(
+    "engine", [_abi.ACO_GEMM_FUSED, _abi.ACO_GEMM_TCGEN05, _abi.ACO_GEMM_MMA_SYNC],
+    ids=["fused", "tcgen05", "mma_sync"])
 
 
 @ENGINES
@@ -78,6 +82,60 @@ def test_gradients_match_cpu_oracle(engine):
         for name in ("W1", "b1", "W2", "b2", "w3", "b3"):
             err = np.linalg.norm(gp[name] - rp[name]) / max(1e-12, np.linalg.norm(rp[name]))
             assert err < 1e-2, (rep, name, err)
+
+
+@pytest.mark.parametrize("E", [1237, 40_000])
+def test_fused_pass_over_many_tiles_matches_oracle(E):
+    """The fused kernel on a ragged set (the last tile part-filled) and on
+    more tiles than SMs (several tiles per CTA, the weight gradients
+    accumulated in tensor memory across them); repeated runs are bit-identical
+    (partials reduced in a fixed order, no atomics)."""
+    rng = np.random.default_rng(E)
+    X = mo.bf16(rng.uniform(-1.0, 2.0, size=(E, 12))).astype(np.float32)
+    y = (rng.random(E) < 0.15).astype(np.float32)
+    pr = EdgePrior(seed=13, engine=_abi.ACO_GEMM_FUSED)
+    lref, gref = mo.loss_and_grads(pr.weights(), X, y, pos_weight=4.0)
+    rp = mo.unpack(gref)
+    first = None
+    for rep in range(3):
+        loss, g = pr.loss_and_grads(X, y, pos_weight=4.0)
+        assert abs(loss - lref) <= 2e-3 * abs(lref)
+        gp = mo.unpack(g)
+        for name in ("W1", "b1", "W2", "b2", "w3", "b3"):
+            err = np.linalg.norm(gp[name] - rp[name]) / max(1e-12, np.linalg.norm(rp[name]))
+            assert err < 1e-2, (rep, name, err)
+        if first is None:
+            first = (loss, g.copy())
+        else:
+            assert loss == first[0] and np.array_equal(g, first[1])
+    p = pr.predict(X)
+    assert np.max(np.abs(p - mo.predict(pr.weights(), X))) < 5e-3
+    pr.close()
+
+
+def test_training_engines_agree_and_fused_is_deterministic():
+    """Two epochs on the same examples: the fused engine and the two layered
+    engines follow the same loss curve (different summation orders only),
+    and two fused runs end with bit-identical weights."""
+    c, _, _, _ = colony(400, 31, k=20, m=60)
+    c.run(20)
+    runs = {}
+    for name, eng in (("fused", _abi.ACO_GEMM_FUSED), ("fused2", _abi.ACO_GEMM_FUSED),
+                      ("tcgen05", _abi.ACO_GEMM_TCGEN05), ("mma_sync", _abi.ACO_GEMM_MMA_SYNC)):
+        pr = EdgePrior(seed=21, engine=eng)
+        pr.add_examples(c)
+        l1 = pr.train(epochs=1, batch=1024, lr=2e-3, seed=4)
+        l2 = pr.train(epochs=1, batch=1024, lr=2e-3, seed=5)
+        runs[name] = (l1, l2, pr.weights())
+        pr.close()
+    c.close()
+    assert runs["fused"][0] == runs["fused2"][0] and runs["fused"][1] == runs["fused2"][1]
+    assert np.array_equal(runs["fused"][2], runs["fused2"][2])
+    for name in ("tcgen05", "mma_sync"):
+        for k in (0, 1):
+            assert abs(runs[name][k] - runs["fused"][k]) <= 0.02 * runs["fused"][k], (name, k)
+        dw = np.linalg.norm(runs[name][2] - runs["fused"][2]) / np.linalg.norm(runs["fused"][2])
+        assert dw < 2e-2, (name, dw)
 
 
 @ENGINES
@@ -106,27 +164,51 @@ def test_colony_with_prior_matches_oracle():
         assert_same_state(c, q, ctx=f"prior iteration {it}")
 
 
-def _plain_runs(insts, iters, prior=None, floor=0.05, seed=0):
-    best = []
+def _colony_for(x, y, seed):
+    p = _abi.default_params(num_ants=min(len(x), 100), cand_k=20, beta=2.0, rho=0.2, seed=seed,
+                            nn_order=_abi.ACO_NN_STABLE, heuristic=_abi.ACO_HEURISTIC_DEVICE,
+                            fallback=_abi.ACO_FALLBACK_BEST, tau0_mode=_abi.ACO_TAU0_DORIGO)
+    c = aco.Colony(coords=(x, y), params=p, num_ants=p.num_ants)
+    c.initialize()
+    return c
+
+
+def _device_seconds(fn):
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    fn()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t
+
+
+def _equal_time_runs(insts, iters, prior, floor=0.05, seed=0):
+    """Plain: one untimed iteration, then `iters` timed ones (T_plain).
+    Learned: the same untimed iteration, then the prior's inference
+    (features, MLP, heuristic update; T_infer) charged to the same budget,
+    which buys floor((T_plain - T_infer) / t_iter) iterations, t_iter =
+    T_plain / iters from the plain run of the same instance."""
+    plain, learned, spent = [], [], []
     for i, (x, y) in enumerate(insts):
-        p = _abi.default_params(num_ants=min(len(x), 100), cand_k=20, beta=2.0, rho=0.2,
-                                seed=seed + i, nn_order=_abi.ACO_NN_STABLE,
-                                heuristic=_abi.ACO_HEURISTIC_DEVICE,
-                                fallback=_abi.ACO_FALLBACK_BEST, tau0_mode=_abi.ACO_TAU0_DORIGO)
-        c = aco.Colony(coords=(x, y), params=p, num_ants=p.num_ants)
-        c.initialize()
-        if prior is not None:
-            prior.apply(c, floor)
-        c.run(iters)
-        best.append(c.getGlobBestDist())
+        c = _colony_for(x, y, seed + i)
+        c.run(1)  # warm-up, not counted
+        t_plain = _device_seconds(lambda: c.run(iters))
+        plain.append(c.getGlobBestDist())
         c.close()
-    return np.array(best, dtype=np.float64)
+        c = _colony_for(x, y, seed + i)
+        c.run(1)
+        t_infer = _device_seconds(lambda: prior.apply(c, floor))
+        budget = min(iters, max(0, int((t_plain - t_infer) / (t_plain / iters))))
+        c.run(budget)
+        learned.append(c.getGlobBestDist())
+        spent.append((t_infer, budget))
+        c.close()
+    return np.array(plain, np.float64), np.array(learned, np.float64), spent
 
 
 def test_training_learns_and_the_prior_helps():
     """Train on labels from the plain method's best tours, then compare the
-    plain method with and without the prior at the same iteration budget on
-    fresh instances."""
+    plain method with and without the prior at equal GPU time on fresh
+    instances (the learned arm pays for its inference in iterations)."""
     train = [instances.uniform_instance(int(n), seed=500 + i) if i % 2 == 0 else
              instances.clustered_instance(int(n), seed=500 + i)
              for i, n in enumerate(np.linspace(100, 200, 24).astype(int))]
@@ -147,6 +229,6 @@ def test_training_learns_and_the_prior_helps():
     assert last < first
     b.close()
     test = [instances.uniform_instance(300, seed=900 + i) for i in range(6)]
-    plain = _plain_runs(test, 10, seed=3)
-    learned = _plain_runs(test, 10, prior=pr, seed=3)
-    assert learned.mean() < plain.mean(), (learned.mean(), plain.mean())
+    plain, learned, spent = _equal_time_runs(test, 30, pr, seed=3)
+    assert all(b >= 1 for _, b in spent), spent
+    assert learned.mean() < plain.mean(), (learned.mean(), plain.mean(), spent)
