@@ -88,7 +88,8 @@ class AcoTuning(ctypes.Structure):
         ("construct_ms", ctypes.c_float),
         ("rows_ms", ctypes.c_float),
         ("staged_instances", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 3),
+        ("construct_mode", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 

@@ -92,6 +92,7 @@ def lib():
         getattr(L, name).argtypes = [_vp]
     L.aco_batch_run.argtypes = [_vp, ctypes.c_int32]
     L.aco_batch_autotune.argtypes = [_vp, ctypes.POINTER(_abi.AcoTuning)]
+    L.aco_colony_autotune.argtypes = [_vp, ctypes.POINTER(_abi.AcoTuning)]
     L.aco_batch_set_tuning.argtypes = [_vp, ctypes.c_int32, ctypes.c_int32]
     L.aco_batch_get_size.argtypes = [_vp, _i32p]
     L.aco_batch_get_colony.argtypes = [_vp, ctypes.c_int32, ctypes.POINTER(_vp)]
@@ -184,6 +185,15 @@ class Colony:
 
     def synchronize(self):
         self._check(self._L.aco_colony_synchronize(self._h), "synchronize")
+
+    def autotune(self):
+        """Times the construction kernels and launch shapes that build the
+        same tours, keeps the fastest and resets the colony to its
+        initialised state (aco_colony_autotune)."""
+        t = _abi.AcoTuning()
+        self._check(self._L.aco_colony_autotune(self._h, ctypes.byref(t)), "autotune")
+        return {"ants_per_block": t.ants_per_block, "construct_ms": t.construct_ms,
+                "construct_mode": t.construct_mode, "staged": bool(t.staged_instances)}
 
     def _i64(self, fn):
         v = ctypes.c_int64()

@@ -291,7 +291,7 @@ int plan_construction(aco_colony *c) {
       (mode == ACO_CONSTRUCT_ROWS || mode == ACO_CONSTRUCT_AUTO)) {
     const size_t per_ant = rows_ant_bytes(c->n, c->K, c->ldk);
     const size_t avail = (size_t)c->max_smem_optin - 1024;  // static shared memory
-    int ants = (c->m + sms - 1) / sms;
+    int ants = c->tune_warps > 0 ? c->tune_warps : (c->m + sms - 1) / sms;
     ants = std::max(1, std::min(ants, kRowsMaxAnts));
     ants = std::min<int>(ants, (int)(avail / per_ant));
     if (ants < 1) return fail(c, ACO_ERR_UNSUPPORTED, "a long row does not fit in shared memory");
@@ -302,7 +302,7 @@ int plan_construction(aco_colony *c) {
     return ACO_OK;
   }
   if (c->K > 32 || !c->nn16 || mode == ACO_CONSTRUCT_GLOBAL) return ACO_OK;
-  int warps = (c->m + sms - 1) / sms;
+  int warps = c->tune_warps > 0 ? c->tune_warps : (c->m + sms - 1) / sms;
   warps = warps < 1 ? 1 : (warps > kStagedMaxWarps ? kStagedMaxWarps : warps);
   int grid = (c->m + warps - 1) / warps;
   if (grid > sms) grid = sms;
@@ -1201,6 +1201,102 @@ int aco_batch_run(aco_batch *b, int32_t iterations) {
 int aco_batch_synchronize(aco_batch *b) {
   if (!b) return ACO_ERR_INVALID_ARGUMENT;
   return batch_state_check(b);
+}
+
+int aco_colony_autotune(aco_colony *c, aco_tuning *out) {
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+  // Candidates: the kernels and launch shapes that build the same tours.
+  // k <= 32: staged, cluster and direct kernels; the ants (warps) per CTA
+  // of the staged kernel without aging and of the direct kernel (the
+  // cluster kernel and the aging staged kernel keep their plan: their ants
+  // per CTA follow from the cluster size and the blend ants).  k > 32: the
+  // long-row kernel with 1..11 ants per CTA.  Always: the general kernel.
+  struct Cand {
+    int mode, warps;
+  };
+  std::vector<Cand> cands;
+  const int warps_try[6] = {0, 1, 2, 4, 8, 16};
+  if (c->K > 32) {
+    const int ants_try[7] = {0, 1, 2, 4, 6, 8, 11};
+    for (int a : ants_try) cands.push_back({ACO_CONSTRUCT_ROWS, a});
+  } else if (c->nn16) {
+    for (int w : warps_try) {
+      if (w == 0 || !c->p.aging) cands.push_back({ACO_CONSTRUCT_STAGED, w});
+    }
+    cands.push_back({ACO_CONSTRUCT_CLUSTER, 0});
+    for (int w : warps_try) cands.push_back({ACO_CONSTRUCT_DIRECT, w});
+  }
+  cands.push_back({ACO_CONSTRUCT_GLOBAL, 0});
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ACO_CUDA(c, cudaEventCreate(&e0), "event");
+  ACO_CUDA(c, cudaEventCreate(&e1), "event");
+  const int user_mode = c->p.construct_mode, user_warps = c->tune_warps;
+  float best_ms = 1e30f;
+  Cand best{user_mode, user_warps};
+  int status = ACO_OK;
+  for (const Cand &k : cands) {
+    c->p.construct_mode = k.mode;
+    c->tune_warps = k.warps;
+    if (plan_construction(c) != ACO_OK) continue;  // not available at this size
+    const bool match = (k.mode == ACO_CONSTRUCT_STAGED && c->staged) ||
+                       (k.mode == ACO_CONSTRUCT_CLUSTER && c->cluster > 0) ||
+                       (k.mode == ACO_CONSTRUCT_DIRECT && c->direct) ||
+                       (k.mode == ACO_CONSTRUCT_ROWS && c->rows) ||
+                       (k.mode == ACO_CONSTRUCT_GLOBAL && !c->staged && !c->cluster &&
+                        !c->direct && !c->rows);
+    if (!match) continue;
+    // A forced shape equal to the plan's own choice is timed once.
+    if (k.warps > 0 && k.warps != c->staged_warps) continue;
+    float ms = 1e30f;
+    const ColonyDev d = make_dev(c);
+    for (int rep = 0; rep < 2 && status == ACO_OK; rep++) {
+      if (cudaEventRecord(e0, c->stream) != cudaSuccess || launch_construction(c, d) != cudaSuccess ||
+          cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+        status = fail(c, ACO_ERR_CUDA, "tune construct");
+        break;
+      }
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, e0, e1);
+      ms = std::min(ms, t);
+    }
+    if (status != ACO_OK) break;
+    if (int e = device_error(c)) {
+      status = e;
+      break;
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = k;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->p.construct_mode = best.mode;
+  c->tune_warps = best.warps;
+  if (status != ACO_OK) {
+    c->p.construct_mode = user_mode;
+    c->tune_warps = user_warps;
+  }
+  if (int s = plan_construction(c)) return s;
+  if (status != ACO_OK) return status;
+  // The timing launches advanced the ages: back to the initialised state
+  // (the pheromone was never touched), and the captured graph is rebuilt.
+  state_changed(c);
+  const ColonyDev d = make_dev(c);
+  ACO_CUDA(c, launch_init_colony(d, c->stream), "reset");
+  ACO_CUDA(c, launch_pheromone_rows(d, false, false, false, c->stream), "reset rows");
+  ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  if (int e = device_error(c)) return e;
+  drop_graph(c);  // captured with the previous construction launch
+  if (out) {
+    memset(out, 0, sizeof(*out));
+    out->ants_per_block = c->rows || c->staged || c->direct || c->cluster ? c->staged_warps : c->apb;
+    out->construct_ms = best_ms;
+    out->staged_instances = c->staged ? 1 : 0;
+    out->construct_mode = c->p.construct_mode;
+  }
+  return ACO_OK;
 }
 
 int aco_batch_autotune(aco_batch *b, aco_tuning *out) {

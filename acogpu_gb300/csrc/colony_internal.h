@@ -42,6 +42,7 @@ struct aco_colony {
   float *mout = nullptr;
   int t2 = 0;
   int staged_grid = 0, staged_warps = 0;
+  int tune_warps = 0;  // ants per CTA forced by the autotuner (0: the plan's choice)
   int num_sms = 0, max_smem_optin = 0;
   std::vector<void *> allocations;
   bool initialized = false;

@@ -304,7 +304,9 @@ typedef struct aco_tuning {
   float construct_ms;     /* best timed construction launch */
   float rows_ms;          /* best timed row pass */
   int32_t staged_instances; /* instances whose candidate table is staged in shared memory */
-  int32_t reserved[3];
+  int32_t construct_mode;   /* aco_colony_autotune: the construction kernel kept (enum
+                               aco_construct_mode) */
+  int32_t reserved[2];
 } aco_tuning;
 
 ACO_API int aco_batch_create(const aco_params *params, int32_t count, const int32_t *sizes,
@@ -320,6 +322,19 @@ ACO_API int aco_batch_synchronize(aco_batch *b);
  * memory (about n <= 1150) are staged there, per work item, unless the batch
  * parameters ask for ACO_CONSTRUCT_GLOBAL; the others read rows from L2. */
 ACO_API int aco_batch_autotune(aco_batch *b, aco_tuning *out);
+/* One colony: times its construction launch on every kernel and launch shape
+ * that builds the same tours -- k <= 32: the staged, cluster and direct
+ * kernels, with 1..16 ants (warps) per CTA on the staged kernel without aging
+ * and on the direct kernel; k > 32: the long-row kernel with 1..11 ants per
+ * CTA; any k: the general kernel -- keeps the fastest (as if construct_mode
+ * had named it), returns the colony to its initialised state and drops the
+ * captured iteration graph.  Call after aco_colony_initialize, before
+ * running.  Not tuned, by design: the candidate-list length k (it changes
+ * which tours the method builds, so it is a parameter of the method, not of
+ * the launch) and the fallback's second tier (its benefit depends on how
+ * concentrated the pheromone is, which a freshly initialised colony cannot
+ * show; its rule is fixed by variant, see aco_fallback_tier). */
+ACO_API int aco_colony_autotune(aco_colony *c, aco_tuning *out);
 /* ants_per_block 1..16; row_threads 0 (keep) or 64..512 in steps of 32 (warp
  * 0 folds the deposits in order, the other warps stage them). */
 ACO_API int aco_batch_set_tuning(aco_batch *b, int32_t ants_per_block, int32_t row_threads);
