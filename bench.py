@@ -482,6 +482,7 @@ def run_parity(args, rank, world, local):
         "data": "synthetic",
         "config": dict(parity_config(),
                        l2="working set about 370 MB per GPU, larger than L2"),
+        "same_config": True,  # --impl reference runs this exact config and metric
         "ant_steps_per_s": tours_all * (PARITY_N - 1) / dev_s,
         "parity": {"integer_tour_lengths_bit_exact": checked,
                    "iterations_checked_per_instance": PARITY_CHECK_ITERS,
@@ -562,6 +563,7 @@ def run_reference_parity(args, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(parity_config(),
                            l2="working set about 370 MB per GPU, larger than L2"),
+            "same_config": True,
             "cpu_baseline": {"value": v, "unit": "tours/s", "cores": threads, "kind": "port",
                              "sample": f"{done} instance-iterations of the {args.steps} x "
                                        f"{len(ports)} requested (at most {REF_BUDGET_S:.0f} s), "
