@@ -175,13 +175,16 @@ cudaError_t launch_gemm_tn_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat
     return cudaErrorInvalidValue;
   dim3 grid(1, (M + kTcBM - 1) / kTcBM, splits);
   if (N == 128) {
-    static bool configured = false;  // 56 KB is above the 48 KB default limit
-    if (!configured) {
+    // 56 KB is above the 48 KB default limit; the attribute is set per device.
+    static unsigned long long configured = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return cudaErrorInvalidDevice;
+    if (!((configured >> dev) & 1ull)) {
       cudaError_t e = cudaFuncSetAttribute(k_gemm_tn_tc<128>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)tc_smem<128>());
       if (e != cudaSuccess) return e;
-      configured = true;
+      configured |= 1ull << dev;
     }
     k_gemm_tn_tc<128><<<grid, 128, tc_smem<128>(), s>>>(ta, tb, C, ldc, M, N, K, kps, mode, err);
   } else {

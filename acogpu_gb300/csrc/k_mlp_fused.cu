@@ -484,8 +484,11 @@ cudaError_t launch_mlp_fused(bool train, const __nv_bfloat16 *X, int rows,
       !tc::make_map_bf16(&t2, w2b, kHidden, kHidden, kHidden, 128) ||
       !tc::make_map_bf16(&t2t, w2tb, kHidden, kHidden, kHidden, 128))
     return cudaErrorInvalidValue;
-  static bool configured = false;  // above the 48 KB default
-  if (!configured) {
+  // Above the 48 KB default; the attribute is set once per device.
+  static unsigned long long configured = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return cudaErrorInvalidDevice;
+  if (!((configured >> dev) & 1ull)) {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_fused<true>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)fused_smem<true>());
@@ -493,7 +496,7 @@ cudaError_t launch_mlp_fused(bool train, const __nv_bfloat16 *X, int rows,
       e = cudaFuncSetAttribute(k_mlp_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)fused_smem<false>());
     if (e != cudaSuccess) return e;
-    configured = true;
+    configured |= 1ull << dev;
   }
   if (train)
     k_mlp_fused<true><<<grid, kThreadsF, fused_smem<true>(), s>>>(
