@@ -47,6 +47,9 @@ cudaError_t launch_construct(const ColonyDev &c, int ants_per_block, cudaStream_
 // Candidate table staged in shared memory (k <= 32, n <= 2048); at most
 // kStagedMaxWarps warps (ants in flight) per CTA.
 constexpr int kStagedMaxWarps = 16;
+// Warps (ants) per CTA of the batch kernel: 20 fit the register file
+// without spilling (launch bound 640 threads, at most 102 registers).
+constexpr int kBatchMaxWarps = 20;
 // Launches of at most this many warps per CTA may hold 255 registers a thread.
 constexpr int kWideFallbackWarps = 8;
 // Pitch of the candidate rows (nn, eta_nn, tau_nn, choice_nn, nn16) for

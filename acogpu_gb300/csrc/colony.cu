@@ -1307,12 +1307,12 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
   cudaEventCreate(&e1);
   // Ants per CTA: warps of the k <= 32 kernels (launch-bounded to 512
   // threads); ants (scan warps, plus the chain warp) of the long-row kernel.
-  const int apbs_short[5] = {1, 2, 4, 8, 16};
-  const int apbs_rows[5] = {2, 4, 6, 8, 11};
+  const int apbs_short[6] = {1, 2, 4, 8, 16, kBatchMaxWarps};
+  const int apbs_rows[6] = {2, 4, 6, 8, 11, 11};
   const int *apbs = b->rows ? apbs_rows : apbs_short;
   float best_ms = 1e30f;
   int best_apb = b->apb;
-  for (int ai = 0; ai < 5; ai++) {
+  for (int ai = 0; ai < 6; ai++) {
     const int apb = apbs[ai];
     const size_t need = b->rows ? batch_rows_smem_bytes(b->max_n, b->max_ldk_rows, apb) + 1024
                                 : batch_construct_smem_bytes(
@@ -1383,7 +1383,7 @@ int aco_batch_autotune(aco_batch *b, aco_tuning *out) {
 }
 
 int aco_batch_set_tuning(aco_batch *b, int32_t ants_per_block, int32_t row_threads) {
-  if (!b || ants_per_block < 1 || ants_per_block > 16 ||
+  if (!b || ants_per_block < 1 || ants_per_block > kBatchMaxWarps ||
       (row_threads != 0 && (row_threads < 64 || row_threads > 512 || row_threads % 32)))
     return ACO_ERR_INVALID_ARGUMENT;
   b->apb = ants_per_block;

@@ -23,7 +23,7 @@ namespace aco {
 // tabu list in the region.  Shared layout:
 //   [region: table, or per-warp tabu lists][per warp: 32 f32][mbarrier]
 template <bool MULTI, bool AGING, int G>
-__global__ void __launch_bounds__(512) k_batch_construct(const ColonyDev *__restrict__ descs,
+__global__ void __launch_bounds__(kBatchMaxWarps * 32) k_batch_construct(const ColonyDev *__restrict__ descs,
                                                          const int4 *__restrict__ items,
                                                          int num_items, int *queue_head,
                                                          int words, int max_chunks,

@@ -315,7 +315,8 @@ ACO_API int aco_batch_initialize(aco_batch *b);
 /* `iterations` graph-replayed iterations of every instance, asynchronous. */
 ACO_API int aco_batch_run(aco_batch *b, int32_t iterations);
 ACO_API int aco_batch_synchronize(aco_batch *b);
-/* Times the construction launch for 1..16 ants per CTA and the row pass for
+/* Times the construction launch for 1..20 ants per CTA (2..11 on the
+ * long-row batch kernel) and the row pass for
  * 128..512 threads, keeps the fastest, then returns every instance to its
  * initialised state.  Call after aco_batch_initialize, before running.
  * Construction: instances with k <= 32 whose candidate table fits in shared
@@ -335,7 +336,7 @@ ACO_API int aco_batch_autotune(aco_batch *b, aco_tuning *out);
  * concentrated the pheromone is, which a freshly initialised colony cannot
  * show; its rule is fixed by variant, see aco_fallback_tier). */
 ACO_API int aco_colony_autotune(aco_colony *c, aco_tuning *out);
-/* ants_per_block 1..16; row_threads 0 (keep) or 64..512 in steps of 32 (warp
+/* ants_per_block 1..20 (1..11 for long rows); row_threads 0 (keep) or 64..512 in steps of 32 (warp
  * 0 folds the deposits in order, the other warps stage them). */
 ACO_API int aco_batch_set_tuning(aco_batch *b, int32_t ants_per_block, int32_t row_threads);
 ACO_API int aco_batch_get_size(aco_batch *b, int32_t *count);

@@ -57,7 +57,7 @@ def test_batch_instances_match_single_colonies(variant, aging, tune, mode):
     b.initialize()
     if tune:
         t = b.autotune()
-        assert t["ants_per_block"] in (1, 2, 4, 8, 16) and t["row_threads"] in (128, 256, 512)
+        assert t["ants_per_block"] in (1, 2, 4, 8, 16, 20) and t["row_threads"] in (128, 256, 512)
         assert t["staged_instances"] == (0 if mode == _abi.ACO_CONSTRUCT_GLOBAL else len(sizes) - 1)
     iters = 8
     b.run(iters)
@@ -139,6 +139,29 @@ def test_coincident_cities_batch_matches_general_kernel():
             c.constructSolution()
         v = b.colony(i)
         assert np.array_equal(v.tours(), c.tours()), f"instance {i}: tours"
+        assert np.array_equal(v.pheromone().view(np.uint32), c.pheromone().view(np.uint32)), i
+        c.close()
+    b.close()
+
+
+@pytest.mark.parametrize("apb", [16, 20])
+def test_batch_with_many_ants_per_cta(apb):
+    """The largest ants-per-CTA shapes of the batch kernel (20 warps fit its
+    register budget) build the same tours as single colonies."""
+    sizes = [900, 57, 1500, 333]
+    insts = make_instances(sizes, 301)
+    p = fast_params()
+    b = aco.Batch(insts, params=p, num_ants=300)
+    b.initialize()
+    b.set_tuning(apb, 0)
+    b.run(4)
+    b.synchronize()
+    for i, inst in enumerate(insts):
+        c = single(inst, p, i, 300)
+        for _ in range(4):
+            c.constructSolution()
+        v = b.colony(i)
+        assert np.array_equal(v.tours(), c.tours()), f"apb {apb} instance {i}: tours"
         assert np.array_equal(v.pheromone().view(np.uint32), c.pheromone().view(np.uint32)), i
         c.close()
     b.close()
