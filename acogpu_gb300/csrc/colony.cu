@@ -1010,9 +1010,15 @@ int batch_build_items(aco_batch *b) {
   }
   std::vector<int4> items;
   for (int i : order) {
+    // ceil(m / apb) items of nearly equal size (no item far below apb ants,
+    // which would leave most of its CTA's warps idle for a whole tour).
     const int m = b->cols[i]->m;
-    for (int a0 = 0; a0 < m; a0 += b->apb)
-      items.push_back(make_int4(i, a0, std::min(b->apb, m - a0), staged[i]));
+    const int parts = (m + b->apb - 1) / b->apb;
+    for (int q = 0, a0 = 0; q < parts; q++) {
+      const int cnt = m / parts + (q < m % parts ? 1 : 0);
+      items.push_back(make_int4(i, a0, cnt, staged[i]));
+      a0 += cnt;
+    }
   }
   if (b->d_items) cudaFree(b->d_items);
   b->d_items = nullptr;
