@@ -52,10 +52,9 @@ cudaError_t launch_transpose_feats(const __nv_bfloat16 *X, int E, __nv_bfloat16 
 // a multiple of 4): the gradient in packed order, then the loss.
 int mlp_fused_grid(int rows, int sms);
 cudaError_t launch_mlp_fused(bool train, const __nv_bfloat16 *X, int rows,
-                             const __nv_bfloat16 *w1b, const __nv_bfloat16 *w2b,
-                             const __nv_bfloat16 *w2tb, const float *w, const float *labels,
-                             float pos_weight, float norm, float *out, float *part, int part_ld,
-                             int grid, uint32_t *err, cudaStream_t s);
+                             const __nv_bfloat16 *w1b, const __nv_bfloat16 *w2b, const float *w,
+                             const float *labels, float pos_weight, float norm, float *out,
+                             float *part, int part_ld, int grid, uint32_t *err, cudaStream_t s);
 // Sums G partial rows in order into gout / loss_out and, with adam, applies
 // the Adam step and refreshes the BF16 weight copies.
 cudaError_t launch_mlp_reduce(float *part, int G, int ld, bool clear, float *gout, float *loss_out,

@@ -50,11 +50,33 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(const void *tile) {
   return d;
 }
 
+// Shared-memory descriptor of an MN-major operand with 128-byte swizzle.
+// An MN-major atom is 8 K-rows of 64 contiguous M (or N) elements, 128 bytes
+// a row, chunks swizzled by the row like the K-major layout -- so a
+// K-major tile set [rows][64-wide K-tiles] written for one product is, read
+// this way, the MN-major operand of a product whose K runs over those rows:
+// M/N atoms `atom_stride` bytes apart (the K-tiles), 8-row groups 1024
+// bytes apart.  Advancing K by 16 rows adds 2048 bytes to the start.
+__device__ __forceinline__ uint64_t smem_desc_sw128_mn(const void *start, uint32_t atom_stride) {
+  const uint64_t addr = smem_u32(start);
+  uint64_t d = (addr >> 4) & 0x3FFFull;
+  d |= (uint64_t)((atom_stride >> 4) & 0x3FFFu) << 16;  // leading byte offset: M/N atoms
+  d |= (uint64_t)(1024 >> 4) << 32;                     // stride byte offset: 8-row K groups
+  d |= 1ull << 46;                                      // version
+  d |= 2ull << 61;                                      // SWIZZLE_128B
+  return d;
+}
+
 // Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t idesc_bf16(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(kBM >> 4) << 24);
+}
+
+// The same with A and/or B MN-major (bits 15 and 16 of the descriptor).
+__host__ __device__ constexpr uint32_t idesc_bf16_major(int n, bool a_mn, bool b_mn) {
+  return idesc_bf16(n) | (a_mn ? 1u << 15 : 0u) | (b_mn ? 1u << 16 : 0u);
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,

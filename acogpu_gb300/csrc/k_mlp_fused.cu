@@ -6,14 +6,18 @@
 // reads accumulator lanes 32(w % 4).. (the tile's rows) and columns
 // 32(w / 4).. of every 128-column accumulator.  Per tile:
 //   Z1  = X W1^T            (TMEM cols [0,128), K = 16)
-//   H1  = bf16(relu(Z1 + b1)) -> shared memory, row-major and transposed
+//   H1  = bf16(relu(Z1 + b1)) -> shared memory
 //   Z2  = H1 W2^T           (TMEM cols [0,128), K = 128)
 //   H2  = bf16(relu(Z2 + b2)); z = H2 . w3 + b3; p = sigmoid(z)
-//   dz  = w (p - y) / norm; dZ2 = bf16(dz w3 [H2 > 0]) -> shared, both ways
+//   dz  = w (p - y) / norm; dZ2 = bf16(dz w3 [H2 > 0]) -> shared memory
 //   dH1 = dZ2 W2            (TMEM cols [0,128))
 //   dW2 += dZ2^T H1         (TMEM cols [128,256), accumulated over tiles)
-//   dZ1 = bf16(dH1 [H1 > 0]) -> shared, transposed
+//   dZ1 = bf16(dH1 [H1 > 0]) -> shared memory
 //   dW1 += dZ1^T X          (TMEM cols [256,272), accumulated over tiles)
+// Every activation is written once, row-major (one row per edge): the
+// products that contract over the edges (dW2, dW1) and the one that needs
+// W2 rather than W2^T (dH1) read the same tiles as MN-major operands, so no
+// transposed copy exists anywhere.
 // The bias and w3 gradients are column sums over the rows, reduced across
 // each warp's 32 rows by a shuffle reduce-scatter and kept per lane.  At the
 // end every CTA writes its partial gradient (and loss) to its own row of
@@ -21,7 +25,7 @@
 // atomics) and applies the Adam step, refreshing the BF16 weight copies.
 // The BF16 rounding points are those of the layered kernels in k_mlp.cu.
 //
-// Operands come from TMA (X tile, W1, W2, W2^T; 128-byte swizzle) or are
+// Operands come from TMA (X tile, W1, W2; 128-byte swizzle) or are
 // written by the epilogue threads in the same swizzled K-major layout,
 // followed by fence.proxy.async before the MMA that reads them.  Thread 0
 // issues every MMA; completion is tracked by tcgen05.commit on an mbarrier.
@@ -43,7 +47,9 @@ namespace {
 using tc::fence_after_sync;
 using tc::fence_before_sync;
 using tc::idesc_bf16;
+using tc::idesc_bf16_major;
 using tc::smem_desc_sw128;
+using tc::smem_desc_sw128_mn;
 using tc::sw128_offset;
 using tc::tma_load_2d;
 using tc::umma_bf16;
@@ -52,18 +58,15 @@ using tc::wait_bounded;
 
 constexpr int kThreadsF = 512;
 constexpr uint32_t kKT = 128 * 128;  // one 128-row K-tile of BF16 (16 KB)
-constexpr uint32_t kKT16 = 16 * 128;  // one 16-row K-tile (2 KB)
 // Shared-memory map (offsets from a 1024-byte aligned base).
 constexpr uint32_t oX = 0;             // X tile [128 e][64] (features 16..63 zero)
 constexpr uint32_t oW1 = 16 * 1024;    // W1 [128 o][64] (inputs 16..63 zero)
 constexpr uint32_t oW2 = 32 * 1024;    // W2 [128 o][128 i], two K-tiles
-constexpr uint32_t oA = 64 * 1024;     // H1 [e][i] -> dZ2 [e][o] -> dZ1^T [o][e]
+constexpr uint32_t oA = 64 * 1024;     // H1 [e][i], two K-tiles
 constexpr uint32_t oV = 96 * 1024;     // vectors, partial sums, barriers (10 KB)
-constexpr uint32_t oW2t = 106 * 1024;  // W2^T [128 i][128 o]          (training)
-constexpr uint32_t oB = 138 * 1024;    // H1^T [i][e]                  (training)
-constexpr uint32_t oC = 170 * 1024;    // dZ2^T [o][e]                 (training)
-constexpr uint32_t oXT = 202 * 1024;   // X^T [16 f][128 e], two K-tiles (training)
-constexpr uint32_t kEndTrain = 206 * 1024, kEndFwd = 106 * 1024;
+constexpr uint32_t oX1 = 106 * 1024;   // second X tile buffer            (training)
+constexpr uint32_t oC = 122 * 1024;    // dZ2 [e][o] -> dZ1 [e][o]        (training)
+constexpr uint32_t kEndTrain = 154 * 1024, kEndFwd = 106 * 1024;
 
 template <bool TRAIN>
 constexpr size_t fused_smem() {
@@ -75,10 +78,6 @@ __device__ __forceinline__ uint32_t bf2_bits(float lo, float hi) {
   uint32_t u;
   memcpy(&u, &b, 4);
   return u;
-}
-
-__device__ __forceinline__ void st16(unsigned char *p, uint32_t v) {
-  *reinterpret_cast<unsigned short *>(p) = (unsigned short)v;
 }
 
 // Column sums over the warp's 32 rows: lane l returns the sum of a[l] over
@@ -108,15 +107,6 @@ __device__ __forceinline__ void store_row32(unsigned char *op, int r, int c0,
         make_uint4(pk[4 * u], pk[4 * u + 1], pk[4 * u + 2], pk[4 * u + 3]);
 }
 
-// The same 32 values as column `r` (K index) of rows c0..c0+31 of a
-// K-major operand with 128 rows: 32 two-byte stores.
-__device__ __forceinline__ void store_col32(unsigned char *op, int r, int c0,
-                                            const uint32_t (&pk)[16]) {
-  unsigned char *t = op + (r >> 6) * kKT;
-#pragma unroll
-  for (int j = 0; j < 32; j++)
-    st16(t + sw128_offset(c0 + j, r & 63), (j & 1) ? pk[j >> 1] >> 16 : pk[j >> 1]);
-}
 
 // MMAs of a 128 x N product with K = 128 (two K-tiles): A K-tiles kKT
 // apart, B K-tiles b_step apart.
@@ -131,20 +121,36 @@ __device__ __forceinline__ void mma_k128(uint32_t d, const unsigned char *a, con
   }
 }
 
+// MMAs of a product with K = 128 running over the rows of row-major tiles:
+// A and/or B read MN-major (start advanced 16 rows = 2048 bytes a step,
+// M/N atoms the 16 KB K-tiles of the tile set), or A K-major (two K-tiles,
+// 32 bytes a step inside a K-tile).
+__device__ __forceinline__ void mma_rows(uint32_t d, const unsigned char *a, bool a_mn,
+                                         const unsigned char *b, int n, bool accumulate) {
+  const uint32_t idesc = idesc_bf16_major(n, a_mn, true);
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const uint64_t da = a_mn ? smem_desc_sw128_mn(a + j * 2048, kKT)
+                             : smem_desc_sw128(a + (j >> 2) * kKT) + 2 * (j & 3);
+    const uint64_t db = smem_desc_sw128_mn(b + j * 2048, kKT);
+    umma_bf16(d, da, db, idesc, (accumulate || j) ? 1u : 0u);
+  }
+}
+
 }  // namespace
 
 template <bool TRAIN>
 __global__ void __launch_bounds__(kThreadsF, 1)
     k_mlp_fused(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW1,
-                const __grid_constant__ CUtensorMap tmW2, const __grid_constant__ CUtensorMap tmW2t,
+                const __grid_constant__ CUtensorMap tmW2,
                 const float *__restrict__ w, const float *__restrict__ labels, int rows,
                 float pos_weight, float norm, float *__restrict__ out, float *__restrict__ part,
                 int part_ld, uint32_t *err) {
   extern __shared__ __align__(1024) unsigned char smem_f[];
   unsigned char *base = reinterpret_cast<unsigned char *>(
       (reinterpret_cast<uintptr_t>(smem_f) + 1023) & ~uintptr_t(1023));
-  unsigned char *sX = base + oX, *sW1 = base + oW1, *sW2 = base + oW2, *sA = base + oA;
-  unsigned char *sW2t = base + oW2t, *sB = base + oB, *sC = base + oC, *sXT = base + oXT;
+  unsigned char *sX0 = base + oX, *sW1 = base + oW1, *sW2 = base + oW2, *sA = base + oA;
+  unsigned char *sX1 = base + oX1, *sC = base + oC;
   float *b1s = reinterpret_cast<float *>(base + oV);
   float *b2s = b1s + 128, *w3s = b2s + 128;
   float *zpart = w3s + 128;    // [4 column blocks][128 rows]
@@ -184,16 +190,12 @@ __global__ void __launch_bounds__(kThreadsF, 1)
   int tile = blockIdx.x;
   bool x_inflight = false;  // thread 0: a TMA load of X not yet waited for
   if (threadIdx.x == 0 && tile < tiles) {
-    mbar_arrive_expect_tx(bar_w, (TRAIN ? 5u : 3u) * kKT);
+    mbar_arrive_expect_tx(bar_w, 3u * kKT);
     tma_load_2d(sW1, &tmW1, 0, 0, bar_w);
     tma_load_2d(sW2, &tmW2, 0, 0, bar_w);
     tma_load_2d(sW2 + kKT, &tmW2, 64, 0, bar_w);
-    if (TRAIN) {
-      tma_load_2d(sW2t, &tmW2t, 0, 0, bar_w);
-      tma_load_2d(sW2t + kKT, &tmW2t, 64, 0, bar_w);
-    }
     mbar_arrive_expect_tx(bar_x, kKT);
-    tma_load_2d(sX, &tmX, 0, tile * 128, bar_x);
+    tma_load_2d(sX0, &tmX, 0, tile * 128, bar_x);
     x_inflight = true;
   }
 
@@ -201,6 +203,10 @@ __global__ void __launch_bounds__(kThreadsF, 1)
   bool w_ready = false, failed = false;
   float gw3a = 0.0f, gb2a = 0.0f, gb1a = 0.0f, lossa = 0.0f, gb3a = 0.0f;
   for (int it = 0; tile < tiles; tile += gridDim.x, it++) {
+    // Training double-buffers the X tile: dW1 of this tile reads it after
+    // the next tile's copy has been started.
+    unsigned char *sX = (TRAIN && (it & 1)) ? sX1 : sX0;
+    unsigned char *sXn = (TRAIN && !(it & 1)) ? sX1 : sX0;
     // ---- Z1 = X W1^T (covers the previous tile's dW1 as well)
     bool ok = wait_bounded(bar_x, ph_x, err);
     ph_x ^= 1u;
@@ -235,17 +241,6 @@ __global__ void __launch_bounds__(kThreadsF, 1)
         m1 |= ((u & 0x7FFF0000u) ? 1u : 0u) << (2 * i + 1);
       }
       store_row32(sA, row, c0, pk);
-      if (TRAIN) store_col32(sB, row, c0, pk);
-    }
-    if (TRAIN && cb == 1) {  // X^T (B of dW1) from the staged X tile
-      const unsigned char *xr = sX + row * 128;
-      const uint4 lo = *reinterpret_cast<const uint4 *>(xr + ((0 ^ (row & 7)) << 4));
-      const uint4 hi = *reinterpret_cast<const uint4 *>(xr + ((1 ^ (row & 7)) << 4));
-      const uint32_t f[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-      unsigned char *t = sXT + (row >> 6) * kKT16;
-#pragma unroll
-      for (int j = 0; j < 16; j++)
-        st16(t + sw128_offset(j, row & 63), (j & 1) ? f[j >> 1] >> 16 : f[j >> 1]);
     }
     fence_proxy_async();
     fence_before_sync();
@@ -253,7 +248,8 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       failed = true;
       break;
     }
-    // ---- Z2 = H1 W2^T; then prefetch the next X tile (sX is free)
+    // ---- Z2 = H1 W2^T; then prefetch the next X tile (into the other
+    // buffer when training: this one is read again by dW1)
     if (threadIdx.x == 0) {
       fence_after_sync();
       mma_k128(tmem, sA, sW2, kKT, idesc_bf16(128), false);
@@ -261,7 +257,7 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       if (tile + (int)gridDim.x < tiles) {
         fence_proxy_async();
         mbar_arrive_expect_tx(bar_x, kKT);
-        tma_load_2d(sX, &tmX, 0, (tile + gridDim.x) * 128, bar_x);
+        tma_load_2d(sXn, &tmX, 0, (tile + gridDim.x) * 128, bar_x);
         x_inflight = true;
       }
     }
@@ -296,7 +292,7 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       }
       continue;
     }
-    // ---- loss, dz; w3 and b3 gradients; dZ2 (A of dH1, and transposed A of dW2)
+    // ---- loss, dz; w3 and b3 gradients; dZ2 (A of dH1 K-major, of dW2 MN-major)
     const float yv = grow < rows ? labels[grow] : -1.0f;
     float dz = 0.0f;
     if (yv >= 0.0f) {  // rows past the set and padding rows (label -1) add nothing
@@ -314,8 +310,7 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       for (int i = 0; i < 32; i++) d[i] = ((m2 >> i) & 1u) ? dz * w3s[c0 + i] : 0.0f;
 #pragma unroll
       for (int i = 0; i < 16; i++) pk[i] = bf2_bits(d[2 * i], d[2 * i + 1]);
-      store_row32(sA, row, c0, pk);
-      store_col32(sC, row, c0, pk);
+      store_row32(sC, row, c0, pk);
       gb2a += colsum32(d, lane);
 #pragma unroll
       for (int i = 0; i < 32; i++) h[i] *= dz;
@@ -327,17 +322,17 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       failed = true;
       break;
     }
-    // ---- dH1 = dZ2 W2 (B rows: W2^T); dW2 += dZ2^T H1
+    // ---- dH1 = dZ2 W2 (W2 read MN-major); dW2 += dZ2^T H1 (both MN-major)
     if (threadIdx.x == 0) {
       fence_after_sync();
-      mma_k128(tmem, sA, sW2t, kKT, idesc_bf16(128), false);
-      mma_k128(tmem + 128, sC, sB, kKT, idesc_bf16(128), it > 0);
+      mma_rows(tmem, sC, false, sW2, 128, false);
+      mma_rows(tmem + 128, sC, true, sA, 128, it > 0);
       umma_commit(bar_mma);
     }
     ok = wait_bounded(bar_mma, ph_m, err);
     ph_m ^= 1u;
     fence_after_sync();
-    // ---- dZ1 = dH1 [H1 > 0] -> transposed (A of dW1); b1 gradient
+    // ---- dZ1 = dH1 [H1 > 0] -> row-major (MN-major A of dW1); b1 gradient
     {
       float v[32];
       tc::tmem_load_32(tl + (uint32_t)c0, v);
@@ -346,7 +341,7 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       for (int i = 0; i < 32; i++) v[i] = ((m1 >> i) & 1u) ? v[i] : 0.0f;
 #pragma unroll
       for (int i = 0; i < 16; i++) pk[i] = bf2_bits(v[2 * i], v[2 * i + 1]);
-      store_col32(sA, row, c0, pk);
+      store_row32(sC, row, c0, pk);
       gb1a += colsum32(v, lane);
     }
     fence_proxy_async();
@@ -358,7 +353,7 @@ __global__ void __launch_bounds__(kThreadsF, 1)
     // ---- dW1 += dZ1^T X (committed with the next tile's Z1, or the drain)
     if (threadIdx.x == 0) {
       fence_after_sync();
-      mma_k128(tmem + 256, sA, sXT, kKT16, idesc_bf16(16), it > 0);
+      mma_rows(tmem + 256, sC, true, sX, 16, it > 0);
     }
   }
 
@@ -468,21 +463,18 @@ int mlp_fused_grid(int rows, int sms) {
 }
 
 cudaError_t launch_mlp_fused(bool train, const __nv_bfloat16 *X, int rows,
-                             const __nv_bfloat16 *w1b, const __nv_bfloat16 *w2b,
-                             const __nv_bfloat16 *w2tb, const float *w, const float *labels,
-                             float pos_weight, float norm, float *out, float *part, int part_ld,
-                             int grid, uint32_t *err, cudaStream_t s) {
+                             const __nv_bfloat16 *w1b, const __nv_bfloat16 *w2b, const float *w,
+                             const float *labels, float pos_weight, float norm, float *out,
+                             float *part, int part_ld, int grid, uint32_t *err, cudaStream_t s) {
   if (rows < 1 || grid < 1 || grid > (rows + 127) / 128) return cudaErrorInvalidValue;
   if ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(w1b) |
-       reinterpret_cast<uintptr_t>(w2b) | reinterpret_cast<uintptr_t>(w2tb) |
-       reinterpret_cast<uintptr_t>(part)) & 15)
+       reinterpret_cast<uintptr_t>(w2b) | reinterpret_cast<uintptr_t>(part)) & 15)
     return cudaErrorInvalidValue;
   if (train && (part_ld & 3)) return cudaErrorInvalidValue;
-  CUtensorMap tx, t1, t2, t2t;
+  CUtensorMap tx, t1, t2;
   if (!tc::make_map_bf16(&tx, X, rows, kFeatPad, kFeatPad, 128) ||
       !tc::make_map_bf16(&t1, w1b, kHidden, kFeatPad, kFeatPad, 128) ||
-      !tc::make_map_bf16(&t2, w2b, kHidden, kHidden, kHidden, 128) ||
-      !tc::make_map_bf16(&t2t, w2tb, kHidden, kHidden, kHidden, 128))
+      !tc::make_map_bf16(&t2, w2b, kHidden, kHidden, kHidden, 128))
     return cudaErrorInvalidValue;
   // Above the 48 KB default; the attribute is set once per device.
   static unsigned long long configured = 0;
@@ -500,10 +492,10 @@ cudaError_t launch_mlp_fused(bool train, const __nv_bfloat16 *X, int rows,
   }
   if (train)
     k_mlp_fused<true><<<grid, kThreadsF, fused_smem<true>(), s>>>(
-        tx, t1, t2, t2t, w, labels, rows, pos_weight, norm, out, part, part_ld, err);
+        tx, t1, t2, w, labels, rows, pos_weight, norm, out, part, part_ld, err);
   else
     k_mlp_fused<false><<<grid, kThreadsF, fused_smem<false>(), s>>>(
-        tx, t1, t2, t2t, w, labels, rows, pos_weight, norm, out, part, part_ld, err);
+        tx, t1, t2, w, labels, rows, pos_weight, norm, out, part, part_ld, err);
   return cudaGetLastError();
 }
 

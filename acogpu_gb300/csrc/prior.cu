@@ -259,7 +259,7 @@ int fused_pass(aco_prior *p, const __nv_bfloat16 *X, const float *Y, int rows, f
   if (int s = ensure_fused(p, rows)) return s;
   const int G = mlp_fused_grid(rows, p->sms);
   uint32_t *err = reinterpret_cast<uint32_t *>(p->scratch + 2);
-  ACO_PCUDA(p, launch_mlp_fused(Y != nullptr, X, rows, p->w1b, p->w2b, p->w2tb, p->w, Y,
+  ACO_PCUDA(p, launch_mlp_fused(Y != nullptr, X, rows, p->w1b, p->w2b, p->w, Y,
                                 pos_weight, (float)std::max(1, rows), probs, p->part, kPartLd, G,
                                 err, p->stream), "fused mlp");
   if (Y)
@@ -445,7 +445,7 @@ int aco_prior_train(aco_prior *p, int32_t epochs, int32_t batch, float lr, uint6
         if (!(s = ensure_fused(p, valid))) {
           const int G = mlp_fused_grid(valid, p->sms);
           uint32_t *err = reinterpret_cast<uint32_t *>(p->scratch + 2);
-          if (launch_mlp_fused(true, X, valid, p->w1b, p->w2b, p->w2tb, p->w, Y, pos_weight,
+          if (launch_mlp_fused(true, X, valid, p->w1b, p->w2b, p->w, Y, pos_weight,
                                (float)std::max(1, valid), nullptr, p->part, kPartLd, G, err,
                                p->stream) != cudaSuccess)
             s = pfail(p, ACO_ERR_CUDA, "fused mlp");
