@@ -18,8 +18,13 @@
 // products that contract over the edges (dW2, dW1) and the one that needs
 // W2 rather than W2^T (dH1) read the same tiles as MN-major operands, so no
 // transposed copy exists anywhere.
-// The bias and w3 gradients are column sums over the rows, reduced across
-// each warp's 32 rows by a shuffle reduce-scatter and kept per lane.  At the
+// The w3 and b2 gradients are column sums over the rows too, and go to the
+// tensor cores: with H2 and its ReLU mask written row-major, and dz split
+// exactly into two BF16 terms (hi = bf16(dz), lo = bf16(dz - hi)) as the two
+// rows of a 16-row B tile, gw3 = H2^T dz and sum_e mask dz accumulate in
+// TMEM (cols [320,336) and [352,368)), FP32-accurate; gb2 = w3 * the latter.
+// The b1 gradient (over the FP32 dH1) is reduced across each warp's 32 rows
+// by a shuffle reduce-scatter and kept per lane.  At the
 // end every CTA writes its partial gradient (and loss) to its own row of
 // `part`; k_mlp_reduce sums the rows in a fixed order (deterministic, no
 // atomics) and applies the Adam step, refreshing the BF16 weight copies.
@@ -66,7 +71,11 @@ constexpr uint32_t oA = 64 * 1024;     // H1 [e][i], two K-tiles
 constexpr uint32_t oV = 96 * 1024;     // vectors, partial sums, barriers (10 KB)
 constexpr uint32_t oX1 = 106 * 1024;   // second X tile buffer            (training)
 constexpr uint32_t oC = 122 * 1024;    // dZ2 [e][o] -> dZ1 [e][o]        (training)
-constexpr uint32_t kEndTrain = 154 * 1024, kEndFwd = 106 * 1024;
+constexpr uint32_t oH2 = 154 * 1024;   // H2 [e][o]                       (training)
+constexpr uint32_t oM2 = 186 * 1024;   // [H2 > 0] [e][o] as BF16 0 / 1   (training)
+constexpr uint32_t oDZ = 218 * 1024;   // dz hi/lo as rows 0/1 of [16][e] (training)
+constexpr uint32_t kEndTrain = 222 * 1024, kEndFwd = 106 * 1024;
+constexpr uint32_t kColW3 = 320, kColB2 = 352;  // TMEM columns of the two sums
 
 template <bool TRAIN>
 constexpr size_t fused_smem() {
@@ -121,6 +130,24 @@ __device__ __forceinline__ void mma_k128(uint32_t d, const unsigned char *a, con
   }
 }
 
+__device__ __forceinline__ void st16(unsigned char *p, uint32_t v) {
+  *reinterpret_cast<unsigned short *>(p) = (unsigned short)v;
+}
+
+// Column sums over the tile's rows on the tensor cores: D[o][n] +=
+// sum_e A[e][o] B[n][e] with A a row-major activation tile read MN-major and
+// B the 16-row K-major dz tile (two 2 KB K-tiles).
+__device__ __forceinline__ void mma_sums(uint32_t d, const unsigned char *a,
+                                         const unsigned char *bt, bool accumulate) {
+  const uint32_t idesc = idesc_bf16_major(16, true, false);
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const uint64_t da = smem_desc_sw128_mn(a + j * 2048, kKT);
+    const uint64_t db = smem_desc_sw128(bt + (j >> 2) * 2048) + 2 * (j & 3);
+    umma_bf16(d, da, db, idesc, (accumulate || j) ? 1u : 0u);
+  }
+}
+
 // MMAs of a product with K = 128 running over the rows of row-major tiles:
 // A and/or B read MN-major (start advanced 16 rows = 2048 bytes a step,
 // M/N atoms the 16 KB K-tiles of the tile set), or A K-major (two K-tiles,
@@ -151,10 +178,11 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       (reinterpret_cast<uintptr_t>(smem_f) + 1023) & ~uintptr_t(1023));
   unsigned char *sX0 = base + oX, *sW1 = base + oW1, *sW2 = base + oW2, *sA = base + oA;
   unsigned char *sX1 = base + oX1, *sC = base + oC;
+  unsigned char *sH2 = base + oH2, *sM2 = base + oM2, *sDZ = base + oDZ;
   float *b1s = reinterpret_cast<float *>(base + oV);
   float *b2s = b1s + 128, *w3s = b2s + 128;
   float *zpart = w3s + 128;    // [4 column blocks][128 rows]
-  float *colsum = zpart + 512;  // [3 sums][4 lane quadrants][128 columns]
+  float *colsum = zpart + 512;  // [4 lane quadrants][128 columns] (b1 gradient)
   float *red = colsum + 1536;   // [8]
   uint64_t *bar_x = reinterpret_cast<uint64_t *>(red + 8);
   uint64_t *bar_w = bar_x + 1, *bar_mma = bar_x + 2, *bar_drain = bar_x + 3;
@@ -174,6 +202,10 @@ __global__ void __launch_bounds__(kThreadsF, 1)
     mbar_init(bar_mma, 1);
     mbar_init(bar_drain, 1);
     fence_barrier_init();
+  }
+  if (TRAIN && threadIdx.x < 256) {  // dz tile: rows 2..15 stay zero
+    reinterpret_cast<uint4 *>(sDZ)[threadIdx.x] = make_uint4(0u, 0u, 0u, 0u);
+    fence_proxy_async();
   }
   if (threadIdx.x < 128) {
     b1s[threadIdx.x] = w[kParamB1 + threadIdx.x];
@@ -201,12 +233,16 @@ __global__ void __launch_bounds__(kThreadsF, 1)
 
   uint32_t ph_x = 0, ph_m = 0;
   bool w_ready = false, failed = false;
-  float gw3a = 0.0f, gb2a = 0.0f, gb1a = 0.0f, lossa = 0.0f, gb3a = 0.0f;
+  float gb1a = 0.0f, lossa = 0.0f, gb3a = 0.0f;
   for (int it = 0; tile < tiles; tile += gridDim.x, it++) {
     // Training double-buffers the X tile: dW1 of this tile reads it after
     // the next tile's copy has been started.
     unsigned char *sX = (TRAIN && (it & 1)) ? sX1 : sX0;
     unsigned char *sXn = (TRAIN && !(it & 1)) ? sX1 : sX0;
+    const int grow = tile * 128 + row;
+    // The label is first needed after the head; its load is in flight
+    // through the first two products.
+    const float yv = (TRAIN && grow < rows) ? __ldg(labels + grow) : -1.0f;
     // ---- Z1 = X W1^T (covers the previous tile's dW1 as well)
     bool ok = wait_bounded(bar_x, ph_x, err);
     ph_x ^= 1u;
@@ -278,12 +314,22 @@ __global__ void __launch_bounds__(kThreadsF, 1)
         zp = fmaf(h[i], w3s[c0 + i], zp);
       }
       zpart[cb * 128 + row] = zp;
+      if (TRAIN) {  // H2 and its mask, row-major (A of the two column sums)
+        uint32_t ph[16], pm[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          ph[i] = bf2_bits(h[2 * i], h[2 * i + 1]);  // exact: h is BF16 already
+          pm[i] = (((m2 >> (2 * i)) & 1u) ? 0x3F80u : 0u) |
+                  (((m2 >> (2 * i + 1)) & 1u) ? 0x3F800000u : 0u);
+        }
+        store_row32(sH2, row, c0, ph);
+        store_row32(sM2, row, c0, pm);
+      }
     }
     fence_before_sync();
     __syncthreads();
     const float z = (((zpart[row] + zpart[128 + row]) + zpart[256 + row]) + zpart[384 + row]) + b3;
     const float p = 1.0f / (1.0f + __expf(-z));
-    const int grow = tile * 128 + row;
     if (!TRAIN) {
       if (cb == 0 && grow < rows) out[grow] = p;
       if (!__syncthreads_and(ok)) {
@@ -293,7 +339,6 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       continue;
     }
     // ---- loss, dz; w3 and b3 gradients; dZ2 (A of dH1 K-major, of dW2 MN-major)
-    const float yv = grow < rows ? labels[grow] : -1.0f;
     float dz = 0.0f;
     if (yv >= 0.0f) {  // rows past the set and padding rows (label -1) add nothing
       const float wt = yv > 0.5f ? pos_weight : 1.0f;
@@ -303,18 +348,23 @@ __global__ void __launch_bounds__(kThreadsF, 1)
         gb3a += dz;
       }
     }
+    if (cb == 0) {  // dz = hi + lo exactly enough (16 significant bits) for the sums
+      const __nv_bfloat16 hi = __float2bfloat16_rn(dz);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(dz - __bfloat162float(hi));
+      unsigned short hb, lb;
+      memcpy(&hb, &hi, 2);
+      memcpy(&lb, &lo, 2);
+      unsigned char *t = sDZ + (row >> 6) * 2048;
+      st16(t + sw128_offset(0, row & 63), hb);
+      st16(t + sw128_offset(1, row & 63), lb);
+    }
     {
-      float d[32];
       uint32_t pk[16];
 #pragma unroll
-      for (int i = 0; i < 32; i++) d[i] = ((m2 >> i) & 1u) ? dz * w3s[c0 + i] : 0.0f;
-#pragma unroll
-      for (int i = 0; i < 16; i++) pk[i] = bf2_bits(d[2 * i], d[2 * i + 1]);
+      for (int i = 0; i < 16; i++)
+        pk[i] = bf2_bits(((m2 >> (2 * i)) & 1u) ? dz * w3s[c0 + 2 * i] : 0.0f,
+                         ((m2 >> (2 * i + 1)) & 1u) ? dz * w3s[c0 + 2 * i + 1] : 0.0f);
       store_row32(sC, row, c0, pk);
-      gb2a += colsum32(d, lane);
-#pragma unroll
-      for (int i = 0; i < 32; i++) h[i] *= dz;
-      gw3a += colsum32(h, lane);
     }
     fence_proxy_async();
     fence_before_sync();
@@ -327,6 +377,8 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       fence_after_sync();
       mma_rows(tmem, sC, false, sW2, 128, false);
       mma_rows(tmem + 128, sC, true, sA, 128, it > 0);
+      mma_sums(tmem + kColW3, sH2, sDZ, it > 0);
+      mma_sums(tmem + kColB2, sM2, sDZ, it > 0);
       umma_commit(bar_mma);
     }
     ok = wait_bounded(bar_mma, ph_m, err);
@@ -380,6 +432,10 @@ __global__ void __launch_bounds__(kThreadsF, 1)
       tc::tmem_load_16(tl + 256u, v);
 #pragma unroll
       for (int f = 0; f < kFeatures; f++) pr[kParamW1 + row * kFeatures + f] = v[f];
+      tc::tmem_load_16(tl + kColW3, v);  // w3 gradient of hidden unit o = row: hi + lo
+      pr[kParamW3 + row] = v[0] + v[1];
+      tc::tmem_load_16(tl + kColB2, v);  // sum_e [H2 > 0] dz, times w3
+      pr[kParamB2 + row] = w3s[row] * (v[0] + v[1]);
 #pragma unroll
       for (int o = 16; o; o >>= 1) {
         lossa += __shfl_xor_sync(kFull, lossa, o);
@@ -390,16 +446,11 @@ __global__ void __launch_bounds__(kThreadsF, 1)
         red[4 + q] = gb3a;
       }
     }
-    colsum[(0 * 4 + q) * 128 + c0 + lane] = gw3a;
-    colsum[(1 * 4 + q) * 128 + c0 + lane] = gb2a;
-    colsum[(2 * 4 + q) * 128 + c0 + lane] = gb1a;
+    colsum[q * 128 + c0 + lane] = gb1a;
     __syncthreads();
     if (threadIdx.x < 128) {
       const int t = threadIdx.x;
-      const float *s0 = colsum, *s1 = colsum + 512, *s2 = colsum + 1024;
-      pr[kParamW3 + t] = ((s0[t] + s0[128 + t]) + s0[256 + t]) + s0[384 + t];
-      pr[kParamB2 + t] = ((s1[t] + s1[128 + t]) + s1[256 + t]) + s1[384 + t];
-      pr[kParamB1 + t] = ((s2[t] + s2[128 + t]) + s2[256 + t]) + s2[384 + t];
+      pr[kParamB1 + t] = ((colsum[t] + colsum[128 + t]) + colsum[256 + t]) + colsum[384 + t];
     }
     if (threadIdx.x == 0) {
       pr[kParamB3] = ((red[4] + red[5]) + red[6]) + red[7];
