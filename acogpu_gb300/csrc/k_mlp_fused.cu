@@ -20,9 +20,10 @@
 // transposed copy exists anywhere.
 // The w3 and b2 gradients are column sums over the rows too, and go to the
 // tensor cores: with H2 and its ReLU mask written row-major, and dz split
-// exactly into two BF16 terms (hi = bf16(dz), lo = bf16(dz - hi)) as the two
-// rows of a 16-row B tile, gw3 = H2^T dz and sum_e mask dz accumulate in
-// TMEM (cols [320,336) and [352,368)), FP32-accurate; gb2 = w3 * the latter.
+// into two BF16 terms (hi = bf16(dz), lo = bf16(dz - hi): 16 significant
+// bits) as the two rows of a 16-row B tile, gw3 = H2^T dz and
+// sum_e mask dz accumulate in TMEM (cols [320,336) and [352,368)), each
+// product exact in FP32; gb2 = w3 * the latter.
 // The b1 gradient (over the FP32 dH1) is reduced across each warp's 32 rows
 // by a shuffle reduce-scatter and kept per lane.  At the
 // end every CTA writes its partial gradient (and loss) to its own row of
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(kThreadsF, 1)
         gb3a += dz;
       }
     }
-    if (cb == 0) {  // dz = hi + lo exactly enough (16 significant bits) for the sums
+    if (cb == 0) {  // dz ~ hi + lo to 16 significant bits, for the two sums
       const __nv_bfloat16 hi = __float2bfloat16_rn(dz);
       const __nv_bfloat16 lo = __float2bfloat16_rn(dz - __bfloat162float(hi));
       unsigned short hb, lb;
