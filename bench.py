@@ -557,6 +557,16 @@ def run_reference_parity(args, rank):
     for q in ports:
         q.close()
     v = tours / dt
+    # The reference itself is single-threaded: the same algorithm on one core
+    # (one iteration of instance 0, after one untimed iteration), for scale.
+    x0, y0 = insts[0]
+    q1 = oracle.Port(instance_params(p, 0), instances.euc2d_distances(x0, y0), threads=1)
+    q1.initialize()
+    q1.iterate()
+    t1 = time.perf_counter()
+    q1.iterate()
+    v1 = q1.num_valid() / (time.perf_counter() - t1)
+    q1.close()
     return {"metric": "tours/s", "value": v, "unit": "tours/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt * len(ports) / max(1, done), "higher_is_better": True,
@@ -570,7 +580,9 @@ def run_reference_parity(args, rank):
                                        f"after {args.warmup} warm-up, C restatement of the "
                                        f"reference CPU path, {threads} threads"},
             "e2e": {"value": v, "unit": "tours/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "single_core": {"value": v1, "unit": "tours/s", "cores": 1,
+                            "sample": "iteration 2 of instance 0, C restatement, 1 thread"}}
 
 
 BATCH_COUNT, BATCH_CAP, BATCH_K = 512, 1024, 20
