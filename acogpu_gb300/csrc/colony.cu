@@ -1252,7 +1252,8 @@ int aco_colony_autotune(aco_colony *c, aco_tuning *out) {
                        (k.mode == ACO_CONSTRUCT_GLOBAL && !c->staged && !c->cluster &&
                         !c->direct && !c->rows);
     if (!match) continue;
-    // A forced shape equal to the plan's own choice is timed once.
+    // A forced shape the plan had to change (clamped to what fits) is not a
+    // new candidate.
     if (k.warps > 0 && k.warps != c->staged_warps) continue;
     float ms = 1e30f;
     const ColonyDev d = make_dev(c);
