@@ -475,10 +475,13 @@ int aco_colony_create_coords(const aco_params *params, const float *x, const flo
   return ACO_OK;
 }
 
-int aco_colony_initialize(aco_colony *c) {
-  NvtxRange range("aco_colony_initialize");
-  if (c) state_changed(c);
-  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+namespace {
+
+// The device work of aco_colony_initialize, enqueued on the colony's stream
+// (the libm heuristic table, read back to the host, is the one wait); the
+// caller checks the device state before the colony counts as initialised.
+int initialize_enqueue(aco_colony *c) {
+  state_changed(c);
   drop_graph(c);
   c->initialized = false;
   const int n = c->n;
@@ -570,8 +573,16 @@ int aco_colony_initialize(aco_colony *c) {
   ACO_CUDA(c, configure_pheromone_rows(c->ld), "configure rows");
   if (int s0 = plan_construction(c)) return s0;
   ACO_CUDA(c, launch_pheromone_rows(d, false, false, false, c->stream), "choice rows");
-  int s = device_error(c);
-  if (s) return s;
+  return ACO_OK;
+}
+
+}  // namespace
+
+int aco_colony_initialize(aco_colony *c) {
+  NvtxRange range("aco_colony_initialize");
+  if (!c) return ACO_ERR_INVALID_ARGUMENT;
+  if (int s = initialize_enqueue(c)) return s;
+  if (int s = device_error(c)) return s;
   c->initialized = true;
   return ACO_OK;
 }
@@ -1156,10 +1167,38 @@ int aco_batch_initialize(aco_batch *b) {
   batch_drop_graph(b);
   std::vector<ColonyDev> descs;
   std::vector<int2> rowmap;
+  // The instances' setup kernels are small (the greedy tour is one CTA):
+  // they run on a pool of streams, ordered after the batch stream, so that
+  // they overlap, with one wait at the end instead of one per instance.
+  constexpr int kInitStreams = 16;
+  const int npool = (int)std::min<size_t>(kInitStreams, b->cols.size());
+  std::vector<cudaStream_t> pool(npool, nullptr);
+  cudaEvent_t ready = nullptr;
+  int s = ACO_OK;
+  if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventRecord(ready, b->stream) != cudaSuccess)
+    s = bfail(b, ACO_ERR_CUDA, "initialize: event");
+  for (int q = 0; q < npool && !s; q++)
+    if (cudaStreamCreateWithFlags(&pool[q], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamWaitEvent(pool[q], ready, 0) != cudaSuccess)
+      s = bfail(b, ACO_ERR_CUDA, "initialize: streams");
+  for (size_t i = 0; i < b->cols.size() && !s; i++) {
+    aco_colony *c = b->cols[i];
+    c->stream = pool[i % npool];
+    if (int e = initialize_enqueue(c)) s = bfail(b, e, c->err);
+  }
+  for (int q = 0; q < npool; q++)
+    if (pool[q] && cudaStreamSynchronize(pool[q]) != cudaSuccess && !s)
+      s = bfail(b, ACO_ERR_CUDA, "initialize: synchronize");
+  for (aco_colony *c : b->cols) c->stream = b->stream;
+  for (int q = 0; q < npool; q++)
+    if (pool[q]) cudaStreamDestroy(pool[q]);
+  if (ready) cudaEventDestroy(ready);
+  if (s) return s;
   for (size_t i = 0; i < b->cols.size(); i++) {
     aco_colony *c = b->cols[i];
-    int s = aco_colony_initialize(c);
-    if (s) return bfail(b, s, c->err);
+    if (int e = device_error(c)) return bfail(b, e, c->err);
+    c->initialized = true;
     descs.push_back(make_dev(c));
     for (int j = 0; j < c->n; j++) rowmap.push_back(make_int2((int)i, j));
   }
