@@ -103,3 +103,22 @@ def test_mode_values_are_checked_before_any_device_call():
     big = np.zeros((1, 1), np.int32)
     assert L.aco_colony_create(ctypes.byref(p), big.ctypes.data_as(ctypes.c_void_p), 8193, 0,
                                ctypes.byref(h)) == _abi.ACO_ERR_UNSUPPORTED
+
+
+def test_null_handles_are_rejected_without_a_device_call():
+    """The tuners and the prior's engine switch check their handles first."""
+    L = aco.lib()
+    t = _abi.AcoTuning()
+    L.aco_colony_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(_abi.AcoTuning)]
+    L.aco_batch_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(_abi.AcoTuning)]
+    L.aco_prior_set_engine.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    assert L.aco_colony_autotune(None, ctypes.byref(t)) == _abi.ACO_ERR_INVALID_ARGUMENT
+    assert L.aco_batch_autotune(None, ctypes.byref(t)) == _abi.ACO_ERR_INVALID_ARGUMENT
+    for eng in (_abi.ACO_GEMM_MMA_SYNC, _abi.ACO_GEMM_TCGEN05, _abi.ACO_GEMM_FUSED):
+        assert L.aco_prior_set_engine(None, eng) == _abi.ACO_ERR_INVALID_ARGUMENT
+
+
+def test_tuning_layout_matches_c():
+    """aco_tuning: five int/float fields, the construction mode, two reserved."""
+    assert ctypes.sizeof(_abi.AcoTuning) == 32
+    assert _abi.AcoTuning.construct_mode.offset == 20
