@@ -91,9 +91,8 @@ cudaError_t launch_construct_cluster(const ColonyDev &c, int grid, int warps, in
 // one chain warp (k_construct_rows.cu).  Each ant has a region of
 // rows_ant_bytes in shared memory (rows_layout): two buffers of compacted
 // weights and int16 ids (S = rows_slots(K) entries each), the running sums at
-// every 32nd entry, a staging area for one row copied by TMA (pitch P = ldk:
-// choice values, or tau for an ant that blends its fitness, and int16 ids),
-// the tabu bits and a visited byte per city.
+// every 32nd entry, the tabu bits and a visited byte per city.  The scan
+// warps read the rows themselves from L2.
 // The last 32 slots of each buffer are per-lane sinks for the stores of
 // dropped entries (past any chain length).  With aging,
 // launch_construct_rows runs the aging plan first (two launches).
@@ -102,28 +101,26 @@ constexpr int kRowsMaxAnts = 11;
 __host__ __device__ inline int rows_slots(int K) { return (K + 31) / 32 * 32 + 32; }
 struct RowsLayout {
   int S;
-  size_t id_off, bend_off, sw_off, si_off, tw_off, tb_off, bytes;
+  size_t id_off, bend_off, tw_off, tb_off, bytes;
 };
-__host__ __device__ inline RowsLayout rows_layout(int n, int K, int P) {
+__host__ __device__ inline RowsLayout rows_layout(int n, int K) {
   RowsLayout L;
   L.S = rows_slots(K);
   L.id_off = (size_t)L.S * 8;
   L.bend_off = (size_t)L.S * 12;
-  L.sw_off = L.bend_off + ((size_t)L.S / 32 * 4 + 15) / 16 * 16;
-  L.si_off = L.sw_off + (size_t)P * 4;
-  L.tw_off = L.si_off + ((size_t)P * 2 + 15) / 16 * 16;
+  L.tw_off = L.bend_off + ((size_t)L.S / 32 * 4 + 15) / 16 * 16;
   L.tb_off = L.tw_off + (size_t)(((n + 31) / 32 + 3) / 4) * 16;
   L.bytes = L.tb_off + (size_t)(n + 15) / 16 * 16;
   return L;
 }
-__host__ __device__ inline size_t rows_ant_bytes(int n, int K, int P) {
-  const size_t b = rows_layout(n, K, P).bytes;
+__host__ __device__ inline size_t rows_ant_bytes(int n, int K) {
+  const size_t b = rows_layout(n, K).bytes;
   return (b + 127) / 128 * 128 + 16;  // consecutive regions start four banks apart
 }
 cudaError_t configure_construct_rows(size_t smem);
 cudaError_t launch_construct_rows(const ColonyDev &c, int grid, int ants, cudaStream_t s);
 // max_ldk: the largest candidate-row pitch of the batch (every instance's
-// layout fits in rows_ant_bytes(max_n, max_ldk, max_ldk)).
+// layout fits in rows_ant_bytes(max_n, max_ldk), as K <= ldk).
 size_t batch_rows_smem_bytes(int max_n, int max_ldk, int ants);
 cudaError_t configure_batch_construct_rows(size_t smem);
 int batch_rows_blocks_per_sm(int ants, size_t smem, bool aging);

@@ -289,7 +289,7 @@ int plan_construction(aco_colony *c) {
   const int sms = c->num_sms > 0 ? c->num_sms : 1;
   if (c->nn16 && c->n <= kRowsMaxCities && c->K > 32 &&
       (mode == ACO_CONSTRUCT_ROWS || mode == ACO_CONSTRUCT_AUTO)) {
-    const size_t per_ant = rows_ant_bytes(c->n, c->K, c->ldk);
+    const size_t per_ant = rows_ant_bytes(c->n, c->K);
     const size_t avail = (size_t)c->max_smem_optin - 1024;  // static shared memory
     int ants = c->tune_warps > 0 ? c->tune_warps : (c->m + sms - 1) / sms;
     ants = std::max(1, std::min(ants, kRowsMaxAnts));

@@ -18,13 +18,13 @@
 // around it.  A CTA holds A ants (A <= kRowsMaxAnts) of one instance, all at
 // the same step, and A + 1 warps:
 //
-//  * scan warp a (one per ant): one lane copies the row it needs (choice
-//    values, or tau for an ant that blends its fitness -- it reads eta from
-//    L2 -- and the int16 city ids) into the ant's staging area with TMA bulk
-//    copies on an mbarrier; the warp then zeroes the weights of visited cities (a bit per
-//    city in shared memory) and compacts the non-zero weights, in row order,
-//    into one of the ant's two buffers (a lane's offset is the count of the
-//    lanes before it, from three ballots of the count bits);
+//  * scan warp a (one per ant): reads the row it needs straight from L2
+//    (choice values, or tau and eta for an ant that blends its fitness, and
+//    the int16 city ids; 16-byte loads, eight 128-entry chunks in flight a
+//    lane), zeroes the weights of visited cities (a byte per city in shared
+//    memory) and compacts the non-zero weights, in row order, into one of the
+//    ant's two buffers (a lane's offset is the count of the lanes before it,
+//    from three ballots of the count bits);
 //  * the chain warp: lane a adds ant a's compacted weights in order,
 //    s = fl(s + w) (sum_prob += prob_ptr[i], partial_sum += prob_ptr[i],
 //    src/Colony.cu:814,840), writes every running sum over its weight, and
@@ -33,10 +33,9 @@
 //
 // One step: the scan warps hand their buffers to the chain warp (named
 // barrier R).  While the chain runs, each scan warp compacts the row of its
-// guessed pick -- staged by TMA as soon as the guess was made -- into its
-// other buffer, and from that row's weights, still in registers, guesses the
-// pick after it (an approximate prefix: chunk sums, a scan over chunks and
-// lanes, the same crossing rule) and starts the copy of that city's row.
+// guessed pick into its other buffer, and from that row's weights, still in
+// registers, guesses the pick after it (an approximate prefix: chunk sums, a
+// scan over chunks and lanes, the same crossing rule).
 // When the chain is done (named barrier C) the scan warp finds the exact
 // pick: rnd = fl(u * S) (src/Colony.cu:826-828); the first 32-entry block
 // whose recorded end sum exceeds rnd, then in that block the first running
@@ -47,13 +46,14 @@
 // A right guess (nearly always: the approximate and the exact prefix differ
 // by a few ulps) leaves the next row compacted before the chain ends, so row
 // loads and scans stay off the critical path; a wrong one is undone and the
-// row of the real pick is fetched and scanned.
+// row of the real pick is scanned.  (The rows once went through shared memory
+// by TMA bulk copies, one row ahead; reading them from L2 in the scan, with
+// eight loads in flight a lane, measured faster and needs no mbarriers.)
 //
 // Every warp of a CTA passes the two named barriers once per step, n - 1
 // steps per item, with no early exit: an inconsistency is recorded in the
-// colony's error word and the step continues on a stand-in city.  Every
-// mbarrier wait is bounded (kMaxPolls) and records a timeout, and no staging
-// copy is left in flight at the end of an item.
+// colony's error word and the step continues on a stand-in city.  The
+// kernel has no other wait.
 #include "k_construct_steps.cuh"
 
 namespace aco {
@@ -68,16 +68,12 @@ namespace aco {
 //                           overwrites each weight with the running sum
 //   id[2]: 2 x S int16      their city ids
 //   bend:  S/32 f32         running sum at the end of every 32 entries
-//   sw:    P f32            staged row: choice values, or tau for an ant that
-//                           blends its fitness (which reads eta from L2)
-//   si:    P int16          staged row: city ids
 //   tw:    tabu bits        visited cities, 32 a word (words padded to 4; the
 //                           fallback's scans read them)
 //   tb:    tabu bytes       visited cities, 0xff or 0 (the scan's lookups: a
 //                           sign-extended byte is the AND mask itself)
-// The staging mbarriers sit in static shared memory (their place must not
-// depend on an instance's layout).  Buffer b is addressed arithmetically (no
-// array of pointers, which a run-time index would move to local memory).
+// Buffer b is addressed arithmetically (no array of pointers, which a
+// run-time index would move to local memory).
 //
 // Entry i of a compacted buffer (weights, sums and ids alike) sits in slot
 // i / 4 at component (i % 4) ^ ((i / 32) % 4) (rows_swz).  A chunk's stores
@@ -89,29 +85,22 @@ struct RowsAnt {
   float *w0;
   int16_t *id0;
   float *bend;
-  float *sw;
-  int16_t *si;
   uint32_t *tw;
   uint8_t *tb;
-  uint64_t *bar;
   int S;
   __device__ __forceinline__ float *w(int b) const { return w0 + b * S; }
   __device__ __forceinline__ int16_t *id(int b) const { return id0 + b * S; }
 };
 
-__device__ __forceinline__ RowsAnt rows_ant_at(unsigned char *base, int n, int K, int P,
-                                               uint64_t *bar) {
-  const RowsLayout L = rows_layout(n, K, P);
+__device__ __forceinline__ RowsAnt rows_ant_at(unsigned char *base, int n, int K) {
+  const RowsLayout L = rows_layout(n, K);
   RowsAnt r;
   r.S = L.S;
   r.w0 = reinterpret_cast<float *>(base);
   r.id0 = reinterpret_cast<int16_t *>(base + L.id_off);
   r.bend = reinterpret_cast<float *>(base + L.bend_off);
-  r.sw = reinterpret_cast<float *>(base + L.sw_off);
-  r.si = reinterpret_cast<int16_t *>(base + L.si_off);
   r.tw = reinterpret_cast<uint32_t *>(base + L.tw_off);
   r.tb = base + L.tb_off;
-  r.bar = bar;
   return r;
 }
 
@@ -132,31 +121,6 @@ __device__ __forceinline__ void named_bar_arrive(int id, int threads) {
   asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
 constexpr int kBarRowsReady = 1, kBarChainDone = 2;
-
-// ---- scan warp: staging ----------------------------------------------------
-
-// Starts the copy of the row of `city` into the staging area (lane 0; the
-// warp's earlier reads of the area are complete).  Row starts are 128-byte
-// aligned (ldk % 32 == 0) and the sizes multiples of 64 bytes.
-__device__ __forceinline__ void rows_stage(const ColonyDev &c, const RowsAnt &ra, int city,
-                                           bool blend, int lane) {
-  __syncwarp();
-  if (lane == 0) {
-    fence_proxy_async();  // the area's earlier generic-proxy reads come first
-    const size_t off = (size_t)city * c.ldk;
-    const uint32_t wb = (uint32_t)c.ldk * 4u, ib = (uint32_t)c.ldk * 2u;
-    mbar_arrive_expect_tx(ra.bar, wb + ib);
-    tma_load_1d(ra.sw, (blend ? c.tau_nn : c.choice_nn) + off, wb, ra.bar);
-    tma_load_1d(ra.si, c.nn16 + off, ib, ra.bar);
-  }
-}
-
-// Waits (bounded) for the staging copies of the current phase.
-__device__ __forceinline__ void rows_stage_wait(const ColonyDev &c, const RowsAnt &ra,
-                                                uint32_t &phase) {
-  mbar_wait_bounded(ra.bar, phase, c.st);
-  phase ^= 1u;
-}
 
 // ---- scan warp: compaction -------------------------------------------------
 
@@ -192,7 +156,7 @@ __device__ __forceinline__ unsigned rows_mask4(uint4 &wbits, uint2 &ip, int p0, 
 // with a partial sum of chunk l >> 2, then two plain levels), their scan over
 // chunks, the first chunk where the running total passes u * S', then within
 // it the lanes' inclusive scan and the entry of the first lane that passes.
-// Any summation order will do: the guess only decides which row is staged
+// Any summation order will do: the guess only decides which row is scanned
 // early.  Returns the city, or -1.
 template <int JB>
 __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2 (&ip)[JB],
@@ -343,7 +307,7 @@ struct RowsScan {
   int guess;  // approximate pick (u >= 0), or -1
 };
 
-// Steps of the header for the staged row (the copy is complete): into wo/io,
+// Steps of the header for the row of `city`, read from L2: into wo/io,
 // zero-padded to L; with u >= 0 also the approximate pick of that row.  JB
 // chunks of 128 entries per round: all of a round's shared loads first, then
 // every chunk's visited lookups, then the ballots of every chunk, then the
@@ -354,6 +318,8 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
                                               int16_t *io, int L, float u, int lane) {
   const int K = c.K;
   const float *erow = c.eta_nn + (size_t)city * c.ldk;
+  const float *grow = (blend ? c.tau_nn : c.choice_nn) + (size_t)city * c.ldk;
+  const int16_t *irow = c.nn16 + (size_t)city * c.ldk;
   RowsScan r;
   r.cnt = 0;
   r.guess = -1;
@@ -365,12 +331,12 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
 #pragma unroll
     for (int j = 0; j < JB; j++) {
       const int p0 = j0 + j * 128 + lane * 4;
-      const bool in = p0 < K;  // p0 < K <= ldk, ldk % 4 == 0: the four entries are staged
-      ip[j] = in ? *reinterpret_cast<const uint2 *>(ra.si + p0) : make_uint2(0u, 0u);
+      const bool in = p0 < K;  // p0 < K <= ldk, ldk % 4 == 0: the four entries are in the row
+      ip[j] = in ? __ldg(reinterpret_cast<const uint2 *>(irow + p0)) : make_uint2(0u, 0u);
       if (!blend) {
-        q[j] = in ? *reinterpret_cast<const uint4 *>(ra.sw + p0) : make_uint4(0, 0, 0, 0);
+        q[j] = in ? __ldg(reinterpret_cast<const uint4 *>(grow + p0)) : make_uint4(0, 0, 0, 0);
       } else {
-        const float4 t = in ? *reinterpret_cast<const float4 *>(ra.sw + p0)
+        const float4 t = in ? __ldg(reinterpret_cast<const float4 *>(grow + p0))
                             : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 e = in ? __ldg(reinterpret_cast<const float4 *>(erow + p0))
                             : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -542,21 +508,19 @@ __device__ __forceinline__ void rows_chain(float *w, float *bend, int L, float *
 
 // ---- the kernel ----------------------------------------------------------------
 
-// Per-CTA control block in static shared memory: the chain sums, which scan
-// warps hold a valid ant, and the staging mbarriers.
+// Per-CTA control block in static shared memory: the chain sums and which
+// scan warps hold a valid ant.
 struct RowsCtl {
   float S[kRowsMaxAnts];
   int active[kRowsMaxAnts];
-  uint64_t bar[kRowsMaxAnts];
 };
 
 // One item: ants `first` .. `first + count - 1` of the colony (positions in
 // the aging plan's list when PLAN: the valid ants come first), all warps of
-// the CTA.  `region` holds the A per-ant regions; `phase` is this scan
-// warp's staging-mbarrier parity, carried across items.
+// the CTA.  `region` holds the A per-ant regions.
 template <bool AGING, bool PLAN>
 __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int count, unsigned char *region,
-                          size_t ant_bytes, RowsCtl &ctl, uint32_t &phase) {
+                          size_t ant_bytes, RowsCtl &ctl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int A = (blockDim.x >> 5) - 1;  // scan warps; warp A is the chain warp
   const int threads = blockDim.x;
@@ -601,12 +565,11 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
     }
     if (lane == 0) ctl.active[warp] = valid ? 1 : 0;
     const RowsAnt ra =
-        rows_ant_at(region + (size_t)warp * ant_bytes, n, K, c.ldk, &ctl.bar[warp]);
+        rows_ant_at(region + (size_t)warp * ant_bytes, n, K);
     int32_t *trow = valid ? c.tours + (size_t)k * c.ld : nullptr;
     uint32_t akey = 0;
     int cur = 0, start = 0, cnt = 0;
-    int guess = -1;         // predicted pick of the current step (its row is being staged)
-    bool inflight = false;  // a staging copy not yet waited for
+    int guess = -1;  // predicted pick of the current step (its row is scanned early)
     int64_t fallbacks = 0;
     bool ok = true;
     if (valid) {
@@ -622,17 +585,11 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       tw_set(ra.tw, ra.tb, start, true, lane);
       if (lane == 0) trow[0] = start;
       if (AGING && a.blend) a.meanc = c.mean[start];
-      rows_stage(c, ra, start, a.blend, lane);
-      rows_stage_wait(c, ra, phase);
       const RowsScan r0 = rows_scan<8>(c, ra, start, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
                                        rows_chain_len(K, n, 1),
                                        n > 2 ? aco_uniform_key(akey, 1u) : -1.0f, lane);
       cnt = r0.cnt;
-      if (r0.guess >= 0 && n > 2) {
-        guess = r0.guess;
-        rows_stage(c, ra, guess, a.blend, lane);
-        inflight = true;
-      }
+      if (r0.guess >= 0 && n > 2) guess = r0.guess;
     }
     int b = 0;
 #pragma unroll 1
@@ -646,32 +603,25 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       g.cnt = 0;
       g.guess = -1;
       int todo = -1;  // city whose row goes into buffer b ^ 1 in this pass
-      bool staged = false, hit = false;
+      bool ahead = false, hit = false;
       int next = cur;
       float u = 0.0f;
       if (valid) {
         u = aco_uniform_key(akey, (uint32_t)x);
-        if (guess >= 0) {  // its row was staged (x + 1 < n)
+        if (guess >= 0) {  // its row is scanned while the chain runs (x + 1 < n)
           tw_set(ra.tw, ra.tb, guess, true, lane);
           todo = guess;
-          staged = true;
+          ahead = true;
         }
       }
 #pragma unroll 1
       for (int pass = 0; pass < 2; pass++) {
         if (todo >= 0) {
           const float m = (AGING && a.blend) ? c.mean[todo] : 0.0f;
-          rows_stage_wait(c, ra, phase);
-          inflight = false;
           g = rows_scan<8>(c, ra, todo, a.blend, m, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
                            rows_chain_len(K, n, x + 1),
                            x + 2 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : -1.0f, lane);
-          if (g.guess >= 0 && x + 2 < n) {
-            rows_stage(c, ra, g.guess, a.blend, lane);
-            inflight = true;
-          } else {
-            g.guess = -1;
-          }
+          if (!(x + 2 < n)) g.guess = -1;
           todo = -1;
         }
         if (pass == 1) break;
@@ -681,8 +631,8 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         const int i = rows_exact(ra.w(b), ra.bend, cnt, rows_chain_len(K, n, x), ctl.S[warp],
                                  u, lane);
         next = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
-        hit = staged && next >= 0 && next == guess;
-        if (staged && !hit) tw_set(ra.tw, ra.tb, guess, false, lane);  // undo the guess
+        hit = ahead && next >= 0 && next == guess;
+        if (ahead && !hit) tw_set(ra.tw, ra.tb, guess, false, lane);  // undo the guess
         if (next < 0) {
           next = rows_fallback(c, cur, ra.tw, a, lane);
           fallbacks++;
@@ -694,15 +644,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         if (!hit) tw_set(ra.tw, ra.tb, next, true, lane);
         if (lane == 0) trow[x] = next;
         if (AGING && a.blend) a.meanc = c.mean[next];
-        if (!hit && x + 1 < n) {
-          if (inflight) {  // the copy of a row no longer needed
-            rows_stage_wait(c, ra, phase);
-            inflight = false;
-          }
-          rows_stage(c, ra, next, a.blend, lane);
-          inflight = true;
-          todo = next;
-        }
+        if (!hit && x + 1 < n) todo = next;
       }
       if (valid) {
         cnt = g.cnt;
@@ -711,7 +653,6 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       }
       b ^= 1;
     }
-    if (inflight) rows_stage_wait(c, ra, phase);  // no copy outlives the item
     if (valid) {
       __syncwarp();
       int64_t len = 0;
@@ -744,7 +685,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       named_bar_sync(kBarRowsReady, threads);
       if (lane < A && ctl.active[lane]) {
         const RowsAnt ra =
-            rows_ant_at(region + (size_t)lane * ant_bytes, n, K, c.ldk, &ctl.bar[lane]);
+            rows_ant_at(region + (size_t)lane * ant_bytes, n, K);
         rows_chain(ra.w(b), ra.bend, rows_chain_len(K, n, x), &ctl.S[lane]);
       }
       __syncwarp();
@@ -752,16 +693,6 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       b ^= 1;
     }
   }
-}
-
-// The staging mbarriers (once per launch).
-__device__ __forceinline__ void rows_init_bars(RowsCtl &ctl) {
-  const int warp = threadIdx.x >> 5, A = (blockDim.x >> 5) - 1;
-  if (warp < A && (threadIdx.x & 31) == 0) {
-    mbar_init(&ctl.bar[warp], 1);
-    fence_barrier_init();
-  }
-  __syncthreads();
 }
 
 // Single colony: CTA g takes ant groups g, g + grid, ... of A ants (A + 1
@@ -772,11 +703,9 @@ __global__ void __launch_bounds__((kRowsMaxAnts + 1) * 32) k_construct_rows(Colo
   extern __shared__ __align__(16) unsigned char smem_rows[];
   __shared__ RowsCtl ctl;
   const int A = (blockDim.x >> 5) - 1;
-  const size_t ant_bytes = rows_ant_bytes(c.n, c.K, c.ldk);
-  rows_init_bars(ctl);
-  uint32_t phase = 0;
+  const size_t ant_bytes = rows_ant_bytes(c.n, c.K);
   for (int first = blockIdx.x * A; first < c.m; first += gridDim.x * A) {
-    rows_item<AGING, AGING>(c, first, min(A, c.m - first), smem_rows, ant_bytes, ctl, phase);
+    rows_item<AGING, AGING>(c, first, min(A, c.m - first), smem_rows, ant_bytes, ctl);
     __syncthreads();
   }
 }
@@ -791,7 +720,7 @@ cudaError_t configure_construct_rows(size_t smem) {
 }
 
 cudaError_t launch_construct_rows(const ColonyDev &c, int grid, int ants, cudaStream_t s) {
-  const size_t smem = (size_t)ants * rows_ant_bytes(c.n, c.K, c.ldk);
+  const size_t smem = (size_t)ants * rows_ant_bytes(c.n, c.K);
   if (c.aging) {
     cudaError_t e = launch_aging_plan(c, s);
     if (e != cudaSuccess) return e;
@@ -814,9 +743,7 @@ __global__ void __launch_bounds__((kRowsMaxAnts + 1) * 32)
   __shared__ ColonyDev s_desc;
   __shared__ RowsCtl ctl;
   __shared__ int s_item;
-  const size_t ant_bytes = rows_ant_bytes(max_n, max_ldk, max_ldk);
-  rows_init_bars(ctl);
-  uint32_t phase = 0;
+  const size_t ant_bytes = rows_ant_bytes(max_n, max_ldk);
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(queue_head, 1);
     __syncthreads();
@@ -825,13 +752,13 @@ __global__ void __launch_bounds__((kRowsMaxAnts + 1) * 32)
     const int4 w = items[it];
     if (threadIdx.x == 0) s_desc = descs[w.x];
     __syncthreads();
-    rows_item<AGING, AGING>(s_desc, w.y, w.z, smem_brows, ant_bytes, ctl, phase);
+    rows_item<AGING, AGING>(s_desc, w.y, w.z, smem_brows, ant_bytes, ctl);
     __syncthreads();  // s_item, s_desc and the regions are rewritten by the next item
   }
 }
 
 size_t batch_rows_smem_bytes(int max_n, int max_ldk, int ants) {
-  return (size_t)ants * rows_ant_bytes(max_n, max_ldk, max_ldk);
+  return (size_t)ants * rows_ant_bytes(max_n, max_ldk);
 }
 
 cudaError_t configure_batch_construct_rows(size_t smem) {

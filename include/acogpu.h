@@ -123,7 +123,7 @@ enum aco_construct_mode {
   ACO_CONSTRUCT_DIRECT = 3,  /* the staged step loop on rows read from L2; k <= 32, n <= 8192 */
   ACO_CONSTRUCT_CLUSTER = 4, /* the table split over a cluster of ceil(n/1024) CTAs, rows
                                 read through distributed shared memory; k <= 32, n <= 8192 */
-  ACO_CONSTRUCT_ROWS = 5     /* the long-row kernel: rows staged by TMA and compacted by a
+  ACO_CONSTRUCT_ROWS = 5     /* the long-row kernel: rows read from L2 and compacted by a
                                 warp per ant, the roulette's sequential prefix over the
                                 non-zero weights by a chain warp; k > 32, n <= 8192 */
 };

@@ -74,7 +74,7 @@ def test_coincident_cities_full_rows():
 
 def test_blending_ants_after_convergence():
     """Small aging limits so the colony converges early: recruits blend
-    their fitness (tau staged, eta read from L2) for min_ret iterations."""
+    their fitness (tau and eta read from L2) for min_ret iterations."""
     _, _, d = instance(220, 75, kind="clustered")
     p = _abi.default_params(num_ants=90, aging=1, cand_k=0, rho=0.2, beta=2.0, seed=75)
     (p.min_retirement_age, p.max_retirement_age, p.local_performance, p.global_performance,
