@@ -28,19 +28,21 @@
 //  * the chain warp: lane a adds ant a's compacted weights in order,
 //    s = fl(s + w) (sum_prob += prob_ptr[i], partial_sum += prob_ptr[i],
 //    src/Colony.cu:814,840), writes every running sum over its weight, and
-//    records the sum at the end of every 32 entries and the total S.  The A
-//    chains share one instruction stream.
+//    records the sum at the end of every 32 entries and the total S; then
+//    it finds ant a's exact pick (below).  The A chains and picks share one
+//    instruction stream.
 //
-// One step: the scan warps hand their buffers to the chain warp (named
-// barrier R).  While the chain runs, each scan warp compacts the row of its
-// guessed pick into its other buffer, and from that row's weights, still in
-// registers, guesses the pick after it (an approximate prefix: chunk sums, a
-// scan over chunks and lanes, the same crossing rule).
-// When the chain is done (named barrier C) the scan warp finds the exact
-// pick: rnd = fl(u * S) (src/Colony.cu:826-828); the first 32-entry block
-// whose recorded end sum exceeds rnd, then in that block the first running
-// sum with !(sum <= rnd) -- written sum > rnd || rnd is NaN, as in the
-// k <= 32 step loop -- is the pick (sums never decrease).  No crossing
+// One step: the scan warps hand their buffers, with the step's uniform u,
+// to the chain warp (named barrier R).  While the chain runs, each scan warp
+// compacts the row of its guessed pick into its other buffer, and from that
+// row's weights, still in registers, guesses the pick after it (an
+// approximate prefix: chunk sums, a scan over chunks and lanes, the same
+// crossing rule).  After its chain, lane a of the chain warp finds ant a's
+// exact pick: rnd = fl(u * S) (src/Colony.cu:826-828); the first 32-entry
+// block whose recorded end sum exceeds rnd, then in that block the first
+// running sum with !(sum <= rnd) -- written sum > rnd || rnd is NaN, as in
+// the k <= 32 step loop -- is the pick (sums never decrease, so both are
+// binary searches), and hands it back (named barrier C).  No crossing
 // (S <= 0, u * S rounding to S, or S = +inf from an infinite weight) takes
 // the fallback, as the reference does (chooseBestNext / select_local_best).
 // A right guess (nearly always: the approximate and the exact prefix differ
@@ -401,32 +403,32 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
   return r;
 }
 
-// Exact pick (see the header): the first block of 32 whose recorded end sum
-// passes rnd = fl(u * S), then in the running sums pf that the chain warp
-// wrote over that block the first entry with !(pf <= rnd).  Entries past
-// cnt hold S (the padding adds zeros) and are not candidates.  Index, or -1.
-__device__ __forceinline__ int rows_exact(const float *pf, const float *bend, int cnt, int L,
-                                          float S, float u, int lane) {
+// Exact pick (see the header) of one ant by one lane: rnd = fl(u * S), the
+// first block of 32 whose recorded end sum passes rnd, then in the running
+// sums pf that the chain wrote over that block the first entry with
+// !(pf <= rnd).  Entries past cnt hold S (the padding adds zeros) and are not
+// candidates.  The sums never decrease, so both searches are binary (a fixed
+// number of steps, the same in every lane); a NaN rnd (u = 0 with S = +inf,
+// or a NaN sum) passes at the first entry.  Index, or -1.
+__device__ __forceinline__ int rows_exact_lane(const float *pf, const float *bend, int cnt, int L,
+                                               float S, float u) {
   if (S <= 0.0f) return -1;  // chooseBestNext (src/Colony.cu:776-778)
   const float rnd = __fmul_rn(u, S);
-  const bool nan = rnd != rnd;
   const int nb = L >> 5;
-  int blk = -1;
-#pragma unroll 1
-  for (int b0 = 0; b0 < nb; b0 += 32) {
-    const int bb = b0 + lane;
-    const float e = bb < nb ? bend[bb] : 0.0f;
-    const unsigned hit = __ballot_sync(kFull, bb < nb && (e > rnd || nan));
-    if (hit) {
-      blk = b0 + __ffs(hit) - 1;
-      break;
-    }
-  }
-  if (blk < 0) return -1;
-  const int i = blk * 32 + lane;
-  const float v = pf[rows_swz(i)];
-  const unsigned hit = __ballot_sync(kFull, i < cnt && (v > rnd || nan));
-  return hit ? blk * 32 + __ffs(hit) - 1 : -1;
+  if (rnd != rnd) return (nb > 0 && cnt > 0) ? 0 : -1;
+  int blk = 0;  // blocks whose end sum is <= rnd
+  int step = 1;
+  while (step * 2 <= nb) step *= 2;
+  for (; step > 0; step >>= 1)
+    if (blk + step <= nb && bend[blk + step - 1] <= rnd) blk += step;
+  if (blk >= nb) return -1;
+  // The block's last running sum is bend[blk] > rnd: at most 31 entries pass.
+  int e = 0;
+#pragma unroll
+  for (int t = 16; t > 0; t >>= 1)
+    if (pf[rows_swz(blk * 32 + e + t - 1)] <= rnd) e += t;
+  const int i = blk * 32 + e;
+  return i < cnt ? i : -1;
 }
 
 // Marks (or unmarks) a city in both tabu forms.
@@ -477,7 +479,7 @@ __device__ __forceinline__ void rows_chain_add32(float4 *w4, const float4 (&a)[8
 // at the end of every 32 entries in bend, the total in *S.  Four blocks of
 // 32 per trip (their swizzle keys 0..3), each block's weights read while the
 // previous block is added.
-__device__ __forceinline__ void rows_chain(float *w, float *bend, int L, float *S) {
+__device__ __forceinline__ float rows_chain(float *w, float *bend, int L) {
   float4 *w4 = reinterpret_cast<float4 *>(w);
   const int nb = L >> 5;
   float s = 0.0f;
@@ -503,15 +505,18 @@ __device__ __forceinline__ void rows_chain(float *w, float *bend, int L, float *
     ACO_CHAIN_BLOCK(3, v, a)
   }
 #undef ACO_CHAIN_BLOCK
-  *S = s;
+  return s;
 }
 
 // ---- the kernel ----------------------------------------------------------------
 
-// Per-CTA control block in static shared memory: the chain sums and which
-// scan warps hold a valid ant.
+// Per-CTA control block in static shared memory: which scan warps hold a
+// valid ant, and per step what scan warp a hands the chain warp with its
+// buffer (the step's uniform u, the buffer's count) and gets back (the pick).
 struct RowsCtl {
-  float S[kRowsMaxAnts];
+  float u[kRowsMaxAnts];
+  int cnt[kRowsMaxAnts];
+  int next[kRowsMaxAnts];
   int active[kRowsMaxAnts];
 };
 
@@ -594,20 +599,22 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
     int b = 0;
 #pragma unroll 1
     for (int x = 1; x < n; x++) {
+      if (valid && lane == 0) {
+        ctl.u[warp] = aco_uniform_key(akey, (uint32_t)x);
+        ctl.cnt[warp] = cnt;
+      }
       __syncwarp();
       named_bar_arrive(kBarRowsReady, threads);
-      // Pass 0 scans the guessed pick's row (while the chain runs), then finds
-      // the exact pick; pass 1 scans the real pick's row after a wrong or
-      // missing guess.  One call site of the scan serves both.
+      // Pass 0 scans the guessed pick's row (while the chain warp runs the
+      // chain and finds the exact pick); pass 1 scans the real pick's row
+      // after a wrong or missing guess.  One call site of the scan serves both.
       RowsScan g;
       g.cnt = 0;
       g.guess = -1;
       int todo = -1;  // city whose row goes into buffer b ^ 1 in this pass
       bool ahead = false, hit = false;
       int next = cur;
-      float u = 0.0f;
       if (valid) {
-        u = aco_uniform_key(akey, (uint32_t)x);
         if (guess >= 0) {  // its row is scanned while the chain runs (x + 1 < n)
           tw_set(ra.tw, ra.tb, guess, true, lane);
           todo = guess;
@@ -628,9 +635,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         __syncwarp();
         named_bar_sync(kBarChainDone, threads);  // once per step, in pass 0
         if (!valid) break;
-        const int i = rows_exact(ra.w(b), ra.bend, cnt, rows_chain_len(K, n, x), ctl.S[warp],
-                                 u, lane);
-        next = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
+        next = ctl.next[warp];
         hit = ahead && next >= 0 && next == guess;
         if (ahead && !hit) tw_set(ra.tw, ra.tb, guess, false, lane);  // undo the guess
         if (next < 0) {
@@ -678,7 +683,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       }
     }
   } else {
-    // ---- chain warp: lane a runs ant a's chain
+    // ---- chain warp: lane a runs ant a's chain, then finds its exact pick
     int b = 0;
 #pragma unroll 1
     for (int x = 1; x < n; x++) {
@@ -686,7 +691,10 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       if (lane < A && ctl.active[lane]) {
         const RowsAnt ra =
             rows_ant_at(region + (size_t)lane * ant_bytes, n, K);
-        rows_chain(ra.w(b), ra.bend, rows_chain_len(K, n, x), &ctl.S[lane]);
+        const int L = rows_chain_len(K, n, x);
+        const float S = rows_chain(ra.w(b), ra.bend, L);
+        const int i = rows_exact_lane(ra.w(b), ra.bend, ctl.cnt[lane], L, S, ctl.u[lane]);
+        ctl.next[lane] = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
       }
       __syncwarp();
       named_bar_arrive(kBarChainDone, threads);
