@@ -309,45 +309,56 @@ struct RowsScan {
   int guess;  // approximate pick (u >= 0), or -1
 };
 
-// Steps of the header for the row of `city`, read from L2: into wo/io,
-// zero-padded to L; with u >= 0 also the approximate pick of that row.  JB
-// chunks of 128 entries per round: all of a round's shared loads first, then
-// every chunk's visited lookups, then the ballots of every chunk, then the
-// compacting stores.
+// Loads round j0 of a city's row from L2 into registers: lane l takes row
+// positions j0 + 128j + 4l .. +3 of chunk j (16-byte weight loads, 8-byte id
+// loads, all JB chunks before any use).  For an ant that blends its fitness
+// the weights are formed from tau and eta as they arrive.
 template <int JB>
-__device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt &ra, int city,
-                                              bool blend, float meanc, float ratio, float *wo,
-                                              int16_t *io, int L, float u, int lane) {
+__device__ __forceinline__ void rows_load(const ColonyDev &c, int city, int j0, bool blend,
+                                          float meanc, float ratio, int lane, uint4 (&q)[JB],
+                                          uint2 (&ip)[JB]) {
   const int K = c.K;
   const float *erow = c.eta_nn + (size_t)city * c.ldk;
   const float *grow = (blend ? c.tau_nn : c.choice_nn) + (size_t)city * c.ldk;
   const int16_t *irow = c.nn16 + (size_t)city * c.ldk;
+#pragma unroll
+  for (int j = 0; j < JB; j++) {
+    const int p0 = j0 + j * 128 + lane * 4;
+    const bool in = p0 < K;  // p0 < K <= ldk, ldk % 4 == 0: the four entries are in the row
+    ip[j] = in ? __ldg(reinterpret_cast<const uint2 *>(irow + p0)) : make_uint2(0u, 0u);
+    if (!blend) {
+      q[j] = in ? __ldg(reinterpret_cast<const uint4 *>(grow + p0)) : make_uint4(0, 0, 0, 0);
+    } else {
+      const float4 t = in ? __ldg(reinterpret_cast<const float4 *>(grow + p0))
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 e = in ? __ldg(reinterpret_cast<const float4 *>(erow + p0))
+                          : make_float4(0.f, 0.f, 0.f, 0.f);
+      q[j].x = __float_as_uint(blend_fitness(t.x, e.x, meanc, ratio, c.use_alpha, c.alpha));
+      q[j].y = __float_as_uint(blend_fitness(t.y, e.y, meanc, ratio, c.use_alpha, c.alpha));
+      q[j].z = __float_as_uint(blend_fitness(t.z, e.z, meanc, ratio, c.use_alpha, c.alpha));
+      q[j].w = __float_as_uint(blend_fitness(t.w, e.w, meanc, ratio, c.use_alpha, c.alpha));
+    }
+  }
+}
+
+// Steps of the header for the row of `city`: into wo/io, zero-padded to L;
+// with u >= 0 also the approximate pick of that row.  JB chunks of 128
+// entries per round, in q/ip: all of a round's loads first (round 0's already
+// issued by the caller when `loaded`), then every chunk's visited lookups,
+// then the ballots of every chunk, then the compacting stores.
+template <int JB>
+__device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt &ra, int city,
+                                              bool blend, float meanc, float ratio, float *wo,
+                                              int16_t *io, int L, float u, int lane,
+                                              uint4 (&q)[JB], uint2 (&ip)[JB], bool loaded) {
+  const int K = c.K;
   RowsScan r;
   r.cnt = 0;
   r.guess = -1;
 #pragma unroll 1
   for (int j0 = 0; j0 < K; j0 += JB * 128) {
-    uint4 q[JB];
-    uint2 ip[JB];
     unsigned nz[JB];
-#pragma unroll
-    for (int j = 0; j < JB; j++) {
-      const int p0 = j0 + j * 128 + lane * 4;
-      const bool in = p0 < K;  // p0 < K <= ldk, ldk % 4 == 0: the four entries are in the row
-      ip[j] = in ? __ldg(reinterpret_cast<const uint2 *>(irow + p0)) : make_uint2(0u, 0u);
-      if (!blend) {
-        q[j] = in ? __ldg(reinterpret_cast<const uint4 *>(grow + p0)) : make_uint4(0, 0, 0, 0);
-      } else {
-        const float4 t = in ? __ldg(reinterpret_cast<const float4 *>(grow + p0))
-                            : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 e = in ? __ldg(reinterpret_cast<const float4 *>(erow + p0))
-                            : make_float4(0.f, 0.f, 0.f, 0.f);
-        q[j].x = __float_as_uint(blend_fitness(t.x, e.x, meanc, ratio, c.use_alpha, c.alpha));
-        q[j].y = __float_as_uint(blend_fitness(t.y, e.y, meanc, ratio, c.use_alpha, c.alpha));
-        q[j].z = __float_as_uint(blend_fitness(t.z, e.z, meanc, ratio, c.use_alpha, c.alpha));
-        q[j].w = __float_as_uint(blend_fitness(t.w, e.w, meanc, ratio, c.use_alpha, c.alpha));
-      }
-    }
+    if (!(loaded && j0 == 0)) rows_load<JB>(c, city, j0, blend, meanc, ratio, lane, q, ip);
 #pragma unroll
     for (int j = 0; j < JB; j++) {
       const int c0 = j0 + j * 128;
@@ -575,6 +586,11 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
     uint32_t akey = 0;
     int cur = 0, start = 0, cnt = 0;
     int guess = -1;  // predicted pick of the current step (its row is scanned early)
+    // Round 0 of the row of city `pre`, loaded ahead (-1: none): issued once a
+    // step's scan has stored its entries, in flight across the barriers.
+    uint4 rq[8];
+    uint2 rip[8];
+    int pre = -1;
     int64_t fallbacks = 0;
     bool ok = true;
     if (valid) {
@@ -592,9 +608,14 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       if (AGING && a.blend) a.meanc = c.mean[start];
       const RowsScan r0 = rows_scan<8>(c, ra, start, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
                                        rows_chain_len(K, n, 1),
-                                       n > 2 ? aco_uniform_key(akey, 1u) : -1.0f, lane);
+                                       n > 2 ? aco_uniform_key(akey, 1u) : -1.0f, lane, rq, rip,
+                                       false);
       cnt = r0.cnt;
       if (r0.guess >= 0 && n > 2) guess = r0.guess;
+      if (guess >= 0 && !a.blend) {
+        rows_load<8>(c, guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
+        pre = guess;
+      }
     }
     int b = 0;
 #pragma unroll 1
@@ -627,9 +648,15 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
           const float m = (AGING && a.blend) ? c.mean[todo] : 0.0f;
           g = rows_scan<8>(c, ra, todo, a.blend, m, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
                            rows_chain_len(K, n, x + 1),
-                           x + 2 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : -1.0f, lane);
+                           x + 2 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : -1.0f, lane, rq,
+                           rip, todo == pre);
           if (!(x + 2 < n)) g.guess = -1;
           todo = -1;
+          pre = -1;
+          if (g.guess >= 0 && !a.blend) {  // the next step's row, loaded across the barriers
+            rows_load<8>(c, g.guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
+            pre = g.guess;
+          }
         }
         if (pass == 1) break;
         __syncwarp();
