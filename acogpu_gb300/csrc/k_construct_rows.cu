@@ -442,28 +442,43 @@ __device__ __forceinline__ int rows_exact_lane(const float *pf, const float *ben
   return i < cnt ? i : -1;
 }
 
-// Marks (or unmarks) a city in both tabu forms.
-__device__ __forceinline__ void tw_set(uint32_t *tw, uint8_t *tb, int city, bool on, int lane) {
+// Marks (or unmarks) a city visited.  The step path keeps the tabu bytes
+// only (a plain store, no read-modify-write of a bit word).
+__device__ __forceinline__ void tb_set(uint8_t *tb, int city, bool on, int lane) {
   __syncwarp();
-  if (lane == 0) {
-    if (on)
-      tw[city >> 5] |= 1u << (city & 31);
-    else
-      tw[city >> 5] &= ~(1u << (city & 31));
-    tb[city] = on ? 0xffu : 0u;
-  }
+  if (lane == 0) tb[city] = on ? 0xffu : 0u;
   __syncwarp();
 }
 
 // The fallback (rare): out of line, so its code stays out of the step loop's
-// instruction stream.
-__device__ __noinline__ int rows_fallback(const ColonyDev &c, int cur, const uint32_t *tw,
-                                          AntCtx a, int lane) {
+// instruction stream.  It first rebuilds the tabu bits it scans from the
+// tabu bytes (bits of cities >= n stay 0).
+__device__ __noinline__ int rows_fallback(const ColonyDev &c, int cur, uint32_t *tw,
+                                          const uint8_t *tb, AntCtx a, int lane) {
+  const int n = c.n;
+  __syncwarp();
+  for (int w = lane; w < (n + 31) / 32; w += 32) {
+    uint32_t bits = 0u;
+    for (int i = 0; i < 32 && w * 32 + i < n; i++)
+      if (tb[w * 32 + i]) bits |= 1u << i;
+    tw[w] = bits;
+  }
+  __syncwarp();
   return fallback_city(c, cur, tw, a, lane);
 }
 
-__device__ __forceinline__ bool tw_test(const uint32_t *tw, int city) {
-  return (tw[city >> 5] >> (city & 31)) & 1u;
+// Barrier `id` over `threads` threads that also returns the AND of every
+// participant's predicate (bar.red.and); it orders shared memory as
+// bar.sync does.
+__device__ __forceinline__ bool named_bar_red_and(int id, int threads, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(id), "r"(threads)
+      : "memory");
+  return r != 0u;
 }
 
 // ---- chain warp --------------------------------------------------------------
@@ -527,6 +542,7 @@ __device__ __forceinline__ float rows_chain(float *w, float *bend, int L) {
 struct RowsCtl {
   float u[kRowsMaxAnts];
   int cnt[kRowsMaxAnts];
+  int guess[kRowsMaxAnts];
   int next[kRowsMaxAnts];
   int active[kRowsMaxAnts];
 };
@@ -603,7 +619,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         start = n - 1;
       }
       cur = start;
-      tw_set(ra.tw, ra.tb, start, true, lane);
+      tb_set(ra.tb, start, true, lane);
       if (lane == 0) trow[0] = start;
       if (AGING && a.blend) a.meanc = c.mean[start];
       const RowsScan r0 = rows_scan<8>(c, ra, start, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
@@ -620,9 +636,12 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
     int b = 0;
 #pragma unroll 1
     for (int x = 1; x < n; x++) {
-      if (valid && lane == 0) {
-        ctl.u[warp] = aco_uniform_key(akey, (uint32_t)x);
-        ctl.cnt[warp] = cnt;
+      if (lane == 0) {
+        if (valid) {
+          ctl.u[warp] = aco_uniform_key(akey, (uint32_t)x);
+          ctl.cnt[warp] = cnt;
+        }
+        ctl.guess[warp] = valid ? guess : -1;
       }
       __syncwarp();
       named_bar_arrive(kBarRowsReady, threads);
@@ -637,7 +656,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       int next = cur;
       if (valid) {
         if (guess >= 0) {  // its row is scanned while the chain runs (x + 1 < n)
-          tw_set(ra.tw, ra.tb, guess, true, lane);
+          tb_set(ra.tb, guess, true, lane);
           todo = guess;
           ahead = true;
         }
@@ -660,20 +679,22 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         }
         if (pass == 1) break;
         __syncwarp();
-        named_bar_sync(kBarChainDone, threads);  // once per step, in pass 0
+        // Once per step, in pass 0: every ant's pick equal to its guess (the
+        // common case) needs no read of the pick.
+        const bool all_hit = named_bar_red_and(kBarChainDone, threads, true);
         if (!valid) break;
-        next = ctl.next[warp];
+        next = all_hit ? guess : ctl.next[warp];
         hit = ahead && next >= 0 && next == guess;
-        if (ahead && !hit) tw_set(ra.tw, ra.tb, guess, false, lane);  // undo the guess
+        if (ahead && !hit) tb_set(ra.tb, guess, false, lane);  // undo the guess
         if (next < 0) {
-          next = rows_fallback(c, cur, ra.tw, a, lane);
+          next = rows_fallback(c, cur, ra.tw, ra.tb, a, lane);
           fallbacks++;
         }
-        if ((unsigned)next >= (unsigned)n || (!hit && tw_test(ra.tw, next))) {
+        if ((unsigned)next >= (unsigned)n || (!hit && ra.tb[next])) {
           ok = false;  // no unvisited city, or a bad id: cannot happen
           next = cur;
         }
-        if (!hit) tw_set(ra.tw, ra.tb, next, true, lane);
+        if (!hit) tb_set(ra.tb, next, true, lane);
         if (lane == 0) trow[x] = next;
         if (AGING && a.blend) a.meanc = c.mean[next];
         if (!hit && x + 1 < n) todo = next;
@@ -715,16 +736,19 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
 #pragma unroll 1
     for (int x = 1; x < n; x++) {
       named_bar_sync(kBarRowsReady, threads);
+      bool hit = true;  // lanes without an ant vote yes
       if (lane < A && ctl.active[lane]) {
         const RowsAnt ra =
             rows_ant_at(region + (size_t)lane * ant_bytes, n, K);
         const int L = rows_chain_len(K, n, x);
         const float S = rows_chain(ra.w(b), ra.bend, L);
         const int i = rows_exact_lane(ra.w(b), ra.bend, ctl.cnt[lane], L, S, ctl.u[lane]);
-        ctl.next[lane] = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
+        const int nx = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
+        ctl.next[lane] = nx;
+        hit = nx >= 0 && nx == ctl.guess[lane];
       }
       __syncwarp();
-      named_bar_arrive(kBarChainDone, threads);
+      named_bar_red_and(kBarChainDone, threads, hit);
       b ^= 1;
     }
   }
