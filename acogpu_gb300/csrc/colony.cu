@@ -1019,14 +1019,47 @@ int batch_build_items(aco_batch *b) {
   } else {
     b->region_bytes = batch_plan_region(b, b->apb, &staged, &b->staged_count);
   }
+  // The launch shape first: the grid decides how many items make whole waves.
+  if (b->rows) {
+    const size_t smem = batch_rows_smem_bytes(b->max_n, b->max_ldk_rows, b->apb);
+    if (b->apb > kRowsMaxAnts || smem + 1024 > (size_t)b->max_smem_optin)
+      return bfail(b, ACO_ERR_UNSUPPORTED, "too many ants per CTA for the long rows' buffers");
+    ACO_BCUDA(b, configure_batch_construct_rows(smem), "configure batch row construct");
+    b->grid = b->num_sms * batch_rows_blocks_per_sm(b->apb, smem, b->p.aging != 0);
+  } else {
+    const size_t smem = batch_construct_smem_bytes(b->region_bytes, b->apb);
+    ACO_BCUDA(b, configure_batch_construct(smem), "configure batch construct");
+    b->grid = b->num_sms * batch_construct_blocks_per_sm(b->apb, smem, b->max_k > 32, b->sp,
+                                                         b->p.aging != 0);
+  }
+  // ceil(m / apb) items of nearly equal size per instance (no item far below
+  // apb ants, which would leave most of its CTA's warps idle for a whole
+  // tour).  When every instance has the same n and m the items take equally
+  // long, and their count is raised to whole waves of the grid (at most apb
+  // and at least one ant an item): the last wave then runs as many items as
+  // the others, each a little lighter, instead of leaving CTAs idle.
+  const size_t ni = b->cols.size();
+  std::vector<int> parts(ni);
+  bool uniform = true;
+  long total = 0;
+  for (size_t i = 0; i < ni; i++) {
+    const aco_colony *c = b->cols[i];
+    parts[i] = (c->m + b->apb - 1) / b->apb;
+    total += parts[i];
+    uniform = uniform && c->n == b->cols[0]->n && c->m == b->cols[0]->m;
+  }
+  if (uniform && b->grid > 0 && total % b->grid != 0) {
+    const long target = (total + b->grid - 1) / b->grid * b->grid;
+    for (size_t i = 0; i < ni; i++) {
+      const long want = target / (long)ni + ((long)i < target % (long)ni ? 1 : 0);
+      parts[i] = (int)std::max<long>(parts[i], std::min<long>(want, b->cols[i]->m));
+    }
+  }
   std::vector<int4> items;
   for (int i : order) {
-    // ceil(m / apb) items of nearly equal size (no item far below apb ants,
-    // which would leave most of its CTA's warps idle for a whole tour).
     const int m = b->cols[i]->m;
-    const int parts = (m + b->apb - 1) / b->apb;
-    for (int q = 0, a0 = 0; q < parts; q++) {
-      const int cnt = m / parts + (q < m % parts ? 1 : 0);
+    for (int q = 0, a0 = 0; q < parts[i]; q++) {
+      const int cnt = m / parts[i] + (q < m % parts[i] ? 1 : 0);
       items.push_back(make_int4(i, a0, cnt, staged[i]));
       a0 += cnt;
     }
@@ -1037,19 +1070,6 @@ int batch_build_items(aco_batch *b) {
   ACO_BCUDA(b, upload_sync(b, b->d_items, items.data(), items.size() * sizeof(int4)),
             "upload items");
   b->num_items = (int)items.size();
-  if (b->rows) {
-    const size_t smem = batch_rows_smem_bytes(b->max_n, b->max_ldk_rows, b->apb);
-    if (b->apb > kRowsMaxAnts || smem + 1024 > (size_t)b->max_smem_optin)
-      return bfail(b, ACO_ERR_UNSUPPORTED, "too many ants per CTA for the long rows' buffers");
-    ACO_BCUDA(b, configure_batch_construct_rows(smem), "configure batch row construct");
-    b->grid = b->num_sms * batch_rows_blocks_per_sm(b->apb, smem, b->p.aging != 0);
-    batch_drop_graph(b);
-    return ACO_OK;
-  }
-  const size_t smem = batch_construct_smem_bytes(b->region_bytes, b->apb);
-  ACO_BCUDA(b, configure_batch_construct(smem), "configure batch construct");
-  b->grid = b->num_sms * batch_construct_blocks_per_sm(b->apb, smem, b->max_k > 32, b->sp,
-                                                       b->p.aging != 0);
   batch_drop_graph(b);
   return ACO_OK;
 }

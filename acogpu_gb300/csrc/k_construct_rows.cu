@@ -204,16 +204,31 @@ __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2
   const int l0 = hc ? __ffs(hc) - 1 : 0;  // 4 * chunk
   const int js = l0 >> 2;
   const float base = __shfl_sync(kFull, inc - t1, l0);
-  float x = ls[0];
-  uint4 qq = q[0];
-  uint2 ii = ip[0];
-#pragma unroll
-  for (int j = 1; j < JB; j++) {
-    if (js == j) {
-      x = ls[j];
-      qq = q[j];
-      ii = ip[j];
-    }
+  // Chunk js's registers, by a (warp-uniform) branch rather than a chain of
+  // selects over all eight chunks.
+  float x;
+  uint4 qq;
+  uint2 ii;
+  switch (js) {
+#define ACO_GUESS_CHUNK(J) \
+  case J:                  \
+    x = ls[J];             \
+    qq = q[J];             \
+    ii = ip[J];            \
+    break;
+    ACO_GUESS_CHUNK(0)
+    ACO_GUESS_CHUNK(1)
+    ACO_GUESS_CHUNK(2)
+    ACO_GUESS_CHUNK(3)
+    ACO_GUESS_CHUNK(4)
+    ACO_GUESS_CHUNK(5)
+    ACO_GUESS_CHUNK(6)
+    default:
+      x = ls[7];
+      qq = q[7];
+      ii = ip[7];
+      break;
+#undef ACO_GUESS_CHUNK
   }
   float incl = x;
 #pragma unroll
@@ -304,16 +319,24 @@ __device__ __forceinline__ int rows_guess_smem(const float *w, const int16_t *id
   return id[rows_swz(blk * 32 + __ffs(hit) - 1)];
 }
 
+// Chunks of 128 entries of the next step's row loaded ahead, across the
+// barriers (their registers stay live through the whole step).  All eight:
+// loading half of them ahead measured slower, and so did freeing the
+// registers for more ants a CTA (13 to 15 ants spill at their lower
+// register cap).
+constexpr int kRowsAhead = 8;
+
 struct RowsScan {
   int cnt;    // non-zero weights written
   int guess;  // approximate pick (u >= 0), or -1
 };
 
-// Loads round j0 of a city's row from L2 into registers: lane l takes row
-// positions j0 + 128j + 4l .. +3 of chunk j (16-byte weight loads, 8-byte id
-// loads, all JB chunks before any use).  For an ant that blends its fitness
-// the weights are formed from tau and eta as they arrive.
-template <int JB>
+// Loads chunks J0 .. J1 - 1 of round j0 of a city's row from L2 into
+// registers: lane l takes row positions j0 + 128j + 4l .. +3 of chunk j
+// (16-byte weight loads, 8-byte id loads, all before any use).  For an ant
+// that blends its fitness the weights are formed from tau and eta as they
+// arrive.
+template <int JB, int J0 = 0, int J1 = JB>
 __device__ __forceinline__ void rows_load(const ColonyDev &c, int city, int j0, bool blend,
                                           float meanc, float ratio, int lane, uint4 (&q)[JB],
                                           uint2 (&ip)[JB]) {
@@ -322,7 +345,7 @@ __device__ __forceinline__ void rows_load(const ColonyDev &c, int city, int j0, 
   const float *grow = (blend ? c.tau_nn : c.choice_nn) + (size_t)city * c.ldk;
   const int16_t *irow = c.nn16 + (size_t)city * c.ldk;
 #pragma unroll
-  for (int j = 0; j < JB; j++) {
+  for (int j = J0; j < J1; j++) {
     const int p0 = j0 + j * 128 + lane * 4;
     const bool in = p0 < K;  // p0 < K <= ldk, ldk % 4 == 0: the four entries are in the row
     ip[j] = in ? __ldg(reinterpret_cast<const uint2 *>(irow + p0)) : make_uint2(0u, 0u);
@@ -357,41 +380,37 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
   r.guess = -1;
 #pragma unroll 1
   for (int j0 = 0; j0 < K; j0 += JB * 128) {
-    unsigned nz[JB];
-    if (!(loaded && j0 == 0)) rows_load<JB>(c, city, j0, blend, meanc, ratio, lane, q, ip);
+    unsigned nz = 0u;  // keep bits, four a chunk: chunk j at bits 4j .. 4j+3
+    if (loaded && j0 == 0)  // chunks 0 .. kRowsAhead - 1 are in q/ip already
+      rows_load<JB, kRowsAhead, JB>(c, city, j0, blend, meanc, ratio, lane, q, ip);
+    else
+      rows_load<JB>(c, city, j0, blend, meanc, ratio, lane, q, ip);
 #pragma unroll
     for (int j = 0; j < JB; j++) {
       const int c0 = j0 + j * 128;
-      nz[j] = 0u;
       if (c0 < K) {  // warp-uniform
         if (c0 + 128 <= K)
-          nz[j] = rows_mask4<false>(q[j], ip[j], c0 + lane * 4, K, ra.tb);
+          nz |= rows_mask4<false>(q[j], ip[j], c0 + lane * 4, K, ra.tb) << (4 * j);
         else
-          nz[j] = rows_mask4<true>(q[j], ip[j], c0 + lane * 4, K, ra.tb);
+          nz |= rows_mask4<true>(q[j], ip[j], c0 + lane * 4, K, ra.tb) << (4 * j);
       } else {
         q[j] = make_uint4(0, 0, 0, 0);
       }
     }
     if (u >= 0.0f && K <= JB * 128) r.guess = rows_guess_regs<JB>(q, ip, u, lane);
-    // A lane's offset in chunk j: the counts of the lanes before it, from
-    // three ballots of the count bits; every chunk's ballots first.
+    // Chunk by chunk: a lane's offset is the count of the lanes before it,
+    // from three ballots of the count bits; every entry is stored (no
+    // branch): a kept one at its place, a dropped one at this lane's sink
+    // slot past any chain length.
     const unsigned lt = (1u << lane) - 1u;
-    int off[JB], tot[JB];
-#pragma unroll
-    for (int j = 0; j < JB; j++) {
-      const int cl = __popc(nz[j]);
-      const unsigned b0 = __ballot_sync(kFull, cl & 1), b1 = __ballot_sync(kFull, cl & 2),
-                     b2 = __ballot_sync(kFull, cl & 4);
-      off[j] = __popc(b0 & lt) + 2 * __popc(b1 & lt) + 4 * __popc(b2 & lt);
-      tot[j] = __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
-    }
-    // Every entry is stored (no branch): a kept one at its place, a dropped
-    // one at this lane's sink slot past any chain length.
     const int sink = ra.S - 32 + lane;
 #pragma unroll
     for (int j = 0; j < JB; j++) {
-      const int o = r.cnt + off[j];
-      const unsigned kp = nz[j];
+      const unsigned kp = (nz >> (4 * j)) & 0xfu;
+      const int cl = __popc(kp);
+      const unsigned b0 = __ballot_sync(kFull, cl & 1), b1 = __ballot_sync(kFull, cl & 2),
+                     b2 = __ballot_sync(kFull, cl & 4);
+      const int o = r.cnt + __popc(b0 & lt) + 2 * __popc(b1 & lt) + 4 * __popc(b2 & lt);
       const int rk[4] = {0, (int)(kp & 1u), (int)(kp & 1u) + (int)((kp >> 1) & 1u),
                          __popc(kp & 7u)};
       const uint32_t wb[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
@@ -403,7 +422,7 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
         wo[e] = __uint_as_float(wb[t]);
         io[e] = id[t];
       }
-      r.cnt += tot[j];
+      r.cnt += __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
     }
   }
   for (int i = r.cnt + lane; i < L; i += 32) wo[rows_swz(i)] = 0.0f;
@@ -600,6 +619,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         rows_ant_at(region + (size_t)warp * ant_bytes, n, K);
     int32_t *trow = valid ? c.tours + (size_t)k * c.ld : nullptr;
     uint32_t akey = 0;
+    float ux = 0.0f;  // the uniform of the current step (drawn once)
     int cur = 0, start = 0, cnt = 0;
     int guess = -1;  // predicted pick of the current step (its row is scanned early)
     // Round 0 of the row of city `pre`, loaded ahead (-1: none): issued once a
@@ -619,17 +639,17 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         start = n - 1;
       }
       cur = start;
+      ux = aco_uniform_key(akey, 1u);
       tb_set(ra.tb, start, true, lane);
       if (lane == 0) trow[0] = start;
       if (AGING && a.blend) a.meanc = c.mean[start];
       const RowsScan r0 = rows_scan<8>(c, ra, start, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
-                                       rows_chain_len(K, n, 1),
-                                       n > 2 ? aco_uniform_key(akey, 1u) : -1.0f, lane, rq, rip,
-                                       false);
+                                       rows_chain_len(K, n, 1), n > 2 ? ux : -1.0f, lane, rq,
+                                       rip, false);
       cnt = r0.cnt;
       if (r0.guess >= 0 && n > 2) guess = r0.guess;
       if (guess >= 0 && !a.blend) {
-        rows_load<8>(c, guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
+        rows_load<8, 0, kRowsAhead>(c, guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
         pre = guess;
       }
     }
@@ -638,13 +658,14 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
     for (int x = 1; x < n; x++) {
       if (lane == 0) {
         if (valid) {
-          ctl.u[warp] = aco_uniform_key(akey, (uint32_t)x);
+          ctl.u[warp] = ux;
           ctl.cnt[warp] = cnt;
         }
         ctl.guess[warp] = valid ? guess : -1;
       }
       __syncwarp();
       named_bar_arrive(kBarRowsReady, threads);
+      const float un = valid && x + 1 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : 0.0f;
       // Pass 0 scans the guessed pick's row (while the chain warp runs the
       // chain and finds the exact pick); pass 1 scans the real pick's row
       // after a wrong or missing guess.  One call site of the scan serves both.
@@ -666,14 +687,13 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         if (todo >= 0) {
           const float m = (AGING && a.blend) ? c.mean[todo] : 0.0f;
           g = rows_scan<8>(c, ra, todo, a.blend, m, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
-                           rows_chain_len(K, n, x + 1),
-                           x + 2 < n ? aco_uniform_key(akey, (uint32_t)(x + 1)) : -1.0f, lane, rq,
-                           rip, todo == pre);
+                           rows_chain_len(K, n, x + 1), x + 2 < n ? un : -1.0f, lane, rq, rip,
+                           todo == pre);
           if (!(x + 2 < n)) g.guess = -1;
           todo = -1;
           pre = -1;
           if (g.guess >= 0 && !a.blend) {  // the next step's row, loaded across the barriers
-            rows_load<8>(c, g.guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
+            rows_load<8, 0, kRowsAhead>(c, g.guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
             pre = g.guess;
           }
         }
@@ -703,6 +723,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         cnt = g.cnt;
         guess = g.guess;
         cur = next;
+        ux = un;
       }
       b ^= 1;
     }
