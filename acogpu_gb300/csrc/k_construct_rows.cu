@@ -159,10 +159,11 @@ __device__ __forceinline__ unsigned rows_mask4(uint4 &wbits, uint2 &ip, int p0, 
 // chunks, the first chunk where the running total passes u * S', then within
 // it the lanes' inclusive scan and the entry of the first lane that passes.
 // Any summation order will do: the guess only decides which row is scanned
-// early.  Returns the city, or -1.
+// early.  Returns the city, or -1, and its position in the round (128 js +
+// 4 lane + t) in pos.
 template <int JB>
 __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2 (&ip)[JB],
-                                               float u, int lane) {
+                                               float u, int lane, int &pos) {
   static_assert(JB == 8, "the transposing butterfly assumes eight chunks");
   float ls[JB];
 #pragma unroll
@@ -244,13 +245,16 @@ __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2
   const int id[4] = {(int)(ii.x & 0xffffu), (int)(ii.x >> 16), (int)(ii.y & 0xffffu),
                      (int)(ii.y >> 16)};
   float acc = incl - x;
-  int city = -1;
+  int city = -1, tc = 0;
 #pragma unroll
   for (int t = 0; t < 4; t++) {
     acc += w[t];
-    city = (city < 0 && w[t] != 0.0f && acc > rnd) ? id[t] : city;
+    const bool take = city < 0 && w[t] != 0.0f && acc > rnd;
+    city = take ? id[t] : city;
+    tc = take ? t : tc;
   }
   city = __shfl_sync(kFull, city, l);
+  pos = js * 128 + l * 4 + __shfl_sync(kFull, tc, l);
   return (s_ok && hc && hit) ? city : -1;
 }
 
@@ -329,6 +333,7 @@ constexpr int kRowsAhead = 8;
 struct RowsScan {
   int cnt;    // non-zero weights written
   int guess;  // approximate pick (u >= 0), or -1
+  int gidx;   // its index in the compacted buffer (rows of one round)
 };
 
 // Loads chunks J0 .. J1 - 1 of round j0 of a city's row from L2 into
@@ -364,12 +369,14 @@ __device__ __forceinline__ void rows_load(const ColonyDev &c, int city, int j0, 
   }
 }
 
-// Steps of the header for the row of `city`: into wo/io, zero-padded to L;
-// with u >= 0 also the approximate pick of that row.  JB chunks of 128
+// Steps of the header for the row of `city`: into wo (and the city ids
+// into io when IDS), zero-padded to L; with u >= 0 also the approximate pick
+// of that row.  Rows of one round (K <= 128 JB) keep no ids: the guess's
+// index in the compacted buffer stands for it.  JB chunks of 128
 // entries per round, in q/ip: all of a round's loads first (round 0's already
 // issued by the caller when `loaded`), then every chunk's visited lookups,
 // then the ballots of every chunk, then the compacting stores.
-template <int JB>
+template <int JB, bool IDS>
 __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt &ra, int city,
                                               bool blend, float meanc, float ratio, float *wo,
                                               int16_t *io, int L, float u, int lane,
@@ -378,6 +385,7 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
   RowsScan r;
   r.cnt = 0;
   r.guess = -1;
+  r.gidx = -1;
 #pragma unroll 1
   for (int j0 = 0; j0 < K; j0 += JB * 128) {
     unsigned nz = 0u;  // keep bits, four a chunk: chunk j at bits 4j .. 4j+3
@@ -397,7 +405,10 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
         q[j] = make_uint4(0, 0, 0, 0);
       }
     }
-    if (u >= 0.0f && K <= JB * 128) r.guess = rows_guess_regs<JB>(q, ip, u, lane);
+    int gpos = -1;
+    if (u >= 0.0f && K <= JB * 128) r.guess = rows_guess_regs<JB>(q, ip, u, lane, gpos);
+    const int gj = r.guess >= 0 ? gpos >> 7 : -1, gt = gpos & 3;
+    int gi = -1;  // the guess's compacted index, in the lane that holds it
     // Chunk by chunk: a lane's offset is the count of the lanes before it,
     // from three ballots of the count bits; every entry is stored (no
     // branch): a kept one at its place, a dropped one at this lane's sink
@@ -420,10 +431,12 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
       for (int t = 0; t < 4; t++) {
         const int e = rows_swz(((kp >> t) & 1u) ? o + rk[t] : sink);
         wo[e] = __uint_as_float(wb[t]);
-        io[e] = id[t];
+        if (IDS) io[e] = id[t];
       }
+      if (!IDS && j == gj) gi = o + __popc(kp & ((1u << gt) - 1u));
       r.cnt += __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
     }
+    if (!IDS && gj >= 0) r.gidx = __shfl_sync(kFull, gi, (gpos >> 2) & 31);
   }
   for (int i = r.cnt + lane; i < L; i += 32) wo[rows_swz(i)] = 0.0f;
   if (u >= 0.0f && K > JB * 128) {
@@ -484,6 +497,54 @@ __device__ __noinline__ int rows_fallback(const ColonyDev &c, int cur, uint32_t 
   }
   __syncwarp();
   return fallback_city(c, cur, tw, a, lane);
+}
+
+// The city of entry idx of the compacted buffer of `city`'s row, for rows of
+// one round that keep no ids (a pick that was not the guess: rare).  The
+// kept entries are the positions below K whose city is unvisited, in row
+// order, and the tabu bytes are as they were when the row was compacted
+// (the guess's mark is undone first), so counting them again finds it.
+__device__ __noinline__ int rows_city_at(const ColonyDev &c, const uint8_t *tb, int city, int idx,
+                                         int lane) {
+  const int K = c.K;
+  const int16_t *irow = c.nn16 + (size_t)city * c.ldk;
+  __syncwarp();
+  int base = 0;
+  for (int c0 = 0; c0 < K; c0 += 128) {
+    int id[4];
+    unsigned kp = 0u;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const int p = c0 + lane * 4 + t;
+      id[t] = p < K ? (int)irow[p] : 0;
+      if (p < K && tb[id[t]] == 0u) kp |= 1u << t;
+    }
+    const int cl = __popc(kp);
+    int inc = cl;  // inclusive scan of the counts over the lanes
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += y;
+    }
+    const int tot = __shfl_sync(kFull, inc, 31);
+    if (idx < base + tot) {
+      int r = idx - base - (inc - cl);  // rank among this lane's kept entries
+      int found = -1;
+      if (r >= 0 && r < cl) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          if ((kp >> t) & 1u) {
+            if (r == 0 && found < 0) found = id[t];
+            r--;
+          }
+        }
+      }
+      const unsigned m = __ballot_sync(kFull, found >= 0);
+      return m ? __shfl_sync(kFull, found, __ffs(m) - 1) : -1;
+    }
+    base += tot;
+  }
+  return -1;
 }
 
 // Barrier `id` over `threads` threads that also returns the AND of every
@@ -557,19 +618,20 @@ __device__ __forceinline__ float rows_chain(float *w, float *bend, int L) {
 
 // Per-CTA control block in static shared memory: which scan warps hold a
 // valid ant, and per step what scan warp a hands the chain warp with its
-// buffer (the step's uniform u, the buffer's count) and gets back (the pick).
+// buffer (the step's uniform u, the buffer's count, its guess) and gets back
+// (the pick).
 struct RowsCtl {
   float u[kRowsMaxAnts];
   int cnt[kRowsMaxAnts];
-  int guess[kRowsMaxAnts];
-  int next[kRowsMaxAnts];
+  int key[kRowsMaxAnts];   // the guess: its city with ids, else its compacted index (-1: none)
+  int next[kRowsMaxAnts];  // the pick, in the same terms
   int active[kRowsMaxAnts];
 };
 
 // One item: ants `first` .. `first + count - 1` of the colony (positions in
 // the aging plan's list when PLAN: the valid ants come first), all warps of
 // the CTA.  `region` holds the A per-ant regions.
-template <bool AGING, bool PLAN>
+template <bool AGING, bool PLAN, bool IDS>
 __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int count, unsigned char *region,
                           size_t ant_bytes, RowsCtl &ctl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -622,6 +684,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
     float ux = 0.0f;  // the uniform of the current step (drawn once)
     int cur = 0, start = 0, cnt = 0;
     int guess = -1;  // predicted pick of the current step (its row is scanned early)
+    int gidx = -1;   // its index in the current buffer (rows without ids)
     // Round 0 of the row of city `pre`, loaded ahead (-1: none): issued once a
     // step's scan has stored its entries, in flight across the barriers.
     uint4 rq[8];
@@ -643,11 +706,14 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       tb_set(ra.tb, start, true, lane);
       if (lane == 0) trow[0] = start;
       if (AGING && a.blend) a.meanc = c.mean[start];
-      const RowsScan r0 = rows_scan<8>(c, ra, start, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
+      const RowsScan r0 = rows_scan<8, IDS>(c, ra, start, a.blend, a.meanc, a.ratio, ra.w(0), ra.id(0),
                                        rows_chain_len(K, n, 1), n > 2 ? ux : -1.0f, lane, rq,
                                        rip, false);
       cnt = r0.cnt;
-      if (r0.guess >= 0 && n > 2) guess = r0.guess;
+      if (r0.guess >= 0 && n > 2) {
+        guess = r0.guess;
+        gidx = r0.gidx;
+      }
       if (guess >= 0 && !a.blend) {
         rows_load<8, 0, kRowsAhead>(c, guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
         pre = guess;
@@ -661,7 +727,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
           ctl.u[warp] = ux;
           ctl.cnt[warp] = cnt;
         }
-        ctl.guess[warp] = valid ? guess : -1;
+        ctl.key[warp] = valid && guess >= 0 ? (IDS ? guess : gidx) : -1;
       }
       __syncwarp();
       named_bar_arrive(kBarRowsReady, threads);
@@ -686,7 +752,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       for (int pass = 0; pass < 2; pass++) {
         if (todo >= 0) {
           const float m = (AGING && a.blend) ? c.mean[todo] : 0.0f;
-          g = rows_scan<8>(c, ra, todo, a.blend, m, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
+          g = rows_scan<8, IDS>(c, ra, todo, a.blend, m, a.ratio, ra.w(b ^ 1), ra.id(b ^ 1),
                            rows_chain_len(K, n, x + 1), x + 2 < n ? un : -1.0f, lane, rq, rip,
                            todo == pre);
           if (!(x + 2 < n)) g.guess = -1;
@@ -703,9 +769,12 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         // common case) needs no read of the pick.
         const bool all_hit = named_bar_red_and(kBarChainDone, threads, true);
         if (!valid) break;
-        next = all_hit ? guess : ctl.next[warp];
-        hit = ahead && next >= 0 && next == guess;
+        const int key = IDS ? guess : gidx;
+        const int got = all_hit ? key : ctl.next[warp];
+        hit = ahead && got >= 0 && got == key;
+        next = hit ? guess : got;
         if (ahead && !hit) tb_set(ra.tb, guess, false, lane);  // undo the guess
+        if (!IDS && !hit && got >= 0) next = rows_city_at(c, ra.tb, cur, got, lane);
         if (next < 0) {
           next = rows_fallback(c, cur, ra.tw, ra.tb, a, lane);
           fallbacks++;
@@ -722,6 +791,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       if (valid) {
         cnt = g.cnt;
         guess = g.guess;
+        gidx = g.gidx;
         cur = next;
         ux = un;
       }
@@ -764,9 +834,9 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         const int L = rows_chain_len(K, n, x);
         const float S = rows_chain(ra.w(b), ra.bend, L);
         const int i = rows_exact_lane(ra.w(b), ra.bend, ctl.cnt[lane], L, S, ctl.u[lane]);
-        const int nx = i >= 0 ? ra.id(b)[rows_swz(i)] : -1;
+        const int nx = IDS ? (i >= 0 ? ra.id(b)[rows_swz(i)] : -1) : i;
         ctl.next[lane] = nx;
-        hit = nx >= 0 && nx == ctl.guess[lane];
+        hit = nx >= 0 && nx == ctl.key[lane];
       }
       __syncwarp();
       named_bar_red_and(kBarChainDone, threads, hit);
@@ -775,38 +845,57 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
   }
 }
 
+// Rows longer than one round of the scan (K > 1024) keep the city ids in
+// the compacted buffers (their guess is taken from the buffer); shorter ones
+// keep none.
+constexpr int kRowsIdsAbove = 8 * 128;
+
 // Single colony: CTA g takes ant groups g, g + grid, ... of A ants (A + 1
 // warps a CTA).  With aging the ants come from the plan's list (k_aging_plan
 // updated the ages), valid ones first.
-template <bool AGING>
+template <bool AGING, bool IDS>
 __global__ void __launch_bounds__((kRowsMaxAnts + 1) * 32) k_construct_rows(ColonyDev c) {
   extern __shared__ __align__(16) unsigned char smem_rows[];
   __shared__ RowsCtl ctl;
   const int A = (blockDim.x >> 5) - 1;
   const size_t ant_bytes = rows_ant_bytes(c.n, c.K);
   for (int first = blockIdx.x * A; first < c.m; first += gridDim.x * A) {
-    rows_item<AGING, AGING>(c, first, min(A, c.m - first), smem_rows, ant_bytes, ctl);
+    rows_item<AGING, AGING, IDS>(c, first, min(A, c.m - first), smem_rows, ant_bytes, ctl);
     __syncthreads();
   }
 }
 
+template <typename F>
+static cudaError_t set_smem_all(F f0, F f1, F f2, F f3, size_t smem) {
+  const F fs[4] = {f0, f1, f2, f3};
+  for (F f : fs) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t configure_construct_rows(size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_construct_rows<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_construct_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-  return e;
+  return set_smem_all(k_construct_rows<false, false>, k_construct_rows<false, true>,
+                      k_construct_rows<true, false>, k_construct_rows<true, true>, smem);
 }
 
 cudaError_t launch_construct_rows(const ColonyDev &c, int grid, int ants, cudaStream_t s) {
   const size_t smem = (size_t)ants * rows_ant_bytes(c.n, c.K);
+  const bool ids = c.K > kRowsIdsAbove;
   if (c.aging) {
     cudaError_t e = launch_aging_plan(c, s);
     if (e != cudaSuccess) return e;
-    k_construct_rows<true><<<grid, (ants + 1) * 32, smem, s>>>(c);
+    if (ids)
+      k_construct_rows<true, true><<<grid, (ants + 1) * 32, smem, s>>>(c);
+    else
+      k_construct_rows<true, false><<<grid, (ants + 1) * 32, smem, s>>>(c);
   } else {
-    k_construct_rows<false><<<grid, (ants + 1) * 32, smem, s>>>(c);
+    if (ids)
+      k_construct_rows<false, true><<<grid, (ants + 1) * 32, smem, s>>>(c);
+    else
+      k_construct_rows<false, false><<<grid, (ants + 1) * 32, smem, s>>>(c);
   }
   return cudaGetLastError();
 }
@@ -814,8 +903,9 @@ cudaError_t launch_construct_rows(const ColonyDev &c, int grid, int ants, cudaSt
 // ---------------------------------------------------------------------------
 // Batches: CTAs take (instance, first plan position, ant count, -) items from
 // the work queue (largest instances first) until it is empty.  The per-ant
-// regions are sized for the batch's largest instance and candidate row.
-template <bool AGING>
+// regions are sized for the batch's largest instance and candidate row; the
+// ids are kept when the longest candidate row needs them.
+template <bool AGING, bool IDS>
 __global__ void __launch_bounds__((kRowsMaxAnts + 1) * 32)
     k_batch_construct_rows(const ColonyDev *__restrict__ descs, const int4 *__restrict__ items,
                            int num_items, int *queue_head, int max_n, int max_ldk) {
@@ -832,7 +922,7 @@ __global__ void __launch_bounds__((kRowsMaxAnts + 1) * 32)
     const int4 w = items[it];
     if (threadIdx.x == 0) s_desc = descs[w.x];
     __syncthreads();
-    rows_item<AGING, AGING>(s_desc, w.y, w.z, smem_brows, ant_bytes, ctl);
+    rows_item<AGING, AGING, IDS>(s_desc, w.y, w.z, smem_brows, ant_bytes, ctl);
     __syncthreads();  // s_item, s_desc and the regions are rewritten by the next item
   }
 }
@@ -842,34 +932,50 @@ size_t batch_rows_smem_bytes(int max_n, int max_ldk, int ants) {
 }
 
 cudaError_t configure_batch_construct_rows(size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_batch_construct_rows<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_batch_construct_rows<true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return e;
+  return set_smem_all(k_batch_construct_rows<false, false>, k_batch_construct_rows<false, true>,
+                      k_batch_construct_rows<true, false>, k_batch_construct_rows<true, true>,
+                      smem);
 }
 
 int batch_rows_blocks_per_sm(int ants, size_t smem, bool aging) {
-  int blocks = 0;
-  const void *fn = aging ? (const void *)k_batch_construct_rows<true>
-                         : (const void *)k_batch_construct_rows<false>;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, (ants + 1) * 32, smem) !=
-      cudaSuccess)
-    return 1;
-  return blocks > 0 ? blocks : 1;
+  // The smaller of the two variants' occupancies (the launch picks one by
+  // the batch's longest row).
+  const void *fns[2] = {
+      aging ? (const void *)k_batch_construct_rows<true, false>
+            : (const void *)k_batch_construct_rows<false, false>,
+      aging ? (const void *)k_batch_construct_rows<true, true>
+            : (const void *)k_batch_construct_rows<false, true>};
+  int best = 0;
+  for (const void *fn : fns) {
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, (ants + 1) * 32, smem) !=
+        cudaSuccess)
+      return 1;
+    best = best == 0 ? blocks : std::min(best, blocks);
+  }
+  return best > 0 ? best : 1;
 }
 
 cudaError_t launch_batch_construct_rows(const ColonyDev *descs, const int4 *items, int num_items,
                                         int *queue_head, int grid, int ants, int max_n,
                                         int max_ldk, bool aging, cudaStream_t s) {
   const size_t smem = batch_rows_smem_bytes(max_n, max_ldk, ants);
-  if (aging)
-    k_batch_construct_rows<true><<<grid, (ants + 1) * 32, smem, s>>>(descs, items, num_items,
-                                                                     queue_head, max_n, max_ldk);
-  else
-    k_batch_construct_rows<false><<<grid, (ants + 1) * 32, smem, s>>>(descs, items, num_items,
-                                                                      queue_head, max_n, max_ldk);
+  const bool ids = max_ldk > kRowsIdsAbove;
+#define ACO_BATCH_ROWS(AG, ID)                                                            \
+  k_batch_construct_rows<AG, ID><<<grid, (ants + 1) * 32, smem, s>>>(descs, items, num_items, \
+                                                                     queue_head, max_n, max_ldk)
+  if (aging) {
+    if (ids)
+      ACO_BATCH_ROWS(true, true);
+    else
+      ACO_BATCH_ROWS(true, false);
+  } else {
+    if (ids)
+      ACO_BATCH_ROWS(false, true);
+    else
+      ACO_BATCH_ROWS(false, false);
+  }
+#undef ACO_BATCH_ROWS
   return cudaGetLastError();
 }
 
