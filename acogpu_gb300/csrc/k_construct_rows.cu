@@ -155,9 +155,10 @@ __device__ __forceinline__ unsigned rows_mask4(uint4 &wbits, uint2 &ip, int p0, 
 // Approximate pick of a row still in registers (one round of JB = 8 chunks
 // of 128 entries): the chunk sums (a transposing butterfly: each of three
 // levels hands half of a lane's chunk sums to its partner, so lane l ends
-// with a partial sum of chunk l >> 2, then two plain levels), their scan over
-// chunks, the first chunk where the running total passes u * S', then within
-// it the lanes' inclusive scan and the entry of the first lane that passes.
+// with a partial sum of chunk l >> 2, then two plain levels), gathered into
+// every lane and scanned there, the first chunk where the running total
+// passes u * S', then within it the lanes' inclusive scan and the entry of
+// the first lane that passes.
 // Any summation order will do: the guess only decides which row is scanned
 // early.  Returns the city, or -1, and its position in the round (128 js +
 // 4 lane + t) in pos.
@@ -190,21 +191,27 @@ __device__ __forceinline__ int rows_guess_regs(const uint4 (&q)[JB], const uint2
   }
   t1 += __shfl_xor_sync(kFull, t1, 2);
   t1 += __shfl_xor_sync(kFull, t1, 1);  // lane l: the sum of chunk l >> 2
-  float inc = t1;                       // inclusive scan over chunks (lanes 0, 4, .., 28)
+  // Every lane gathers the eight chunk sums (lane 4c holds chunk c's) and
+  // scans them itself: the same values in every lane, so js is uniform.
+  float ct[JB];
 #pragma unroll
-  for (int o = 4; o < 32; o <<= 1) {
-    const float y = __shfl_up_sync(kFull, inc, o);
-    if (lane >= o) inc += y;
-  }
-  // No early return below: every shuffle runs in every case, so the guess's
-  // instructions can interleave with the caller's compaction stores.
-  const float S = __shfl_sync(kFull, inc, 28);
+  for (int cc = 0; cc < JB; cc++) ct[cc] = __shfl_sync(kFull, t1, 4 * cc);
+  const float S = ((ct[0] + ct[1]) + (ct[2] + ct[3])) + ((ct[4] + ct[5]) + (ct[6] + ct[7]));
   const bool s_ok = S > 0.0f && S < INFINITY;
   const float rnd = u * S;
-  const unsigned hc = __ballot_sync(kFull, (lane & 3) == 0 && inc > rnd);
-  const int l0 = hc ? __ffs(hc) - 1 : 0;  // 4 * chunk
-  const int js = l0 >> 2;
-  const float base = __shfl_sync(kFull, inc - t1, l0);
+  int js = -1;
+  float base = 0.0f, acc0 = 0.0f;
+#pragma unroll
+  for (int cc = 0; cc < JB; cc++) {
+    const float nx = acc0 + ct[cc];
+    if (js < 0 && nx > rnd) {
+      js = cc;
+      base = acc0;
+    }
+    acc0 = nx;
+  }
+  const bool hc = js >= 0;
+  if (js < 0) js = 0;
   // Chunk js's registers, by a (warp-uniform) branch rather than a chain of
   // selects over all eight chunks.
   float x;
