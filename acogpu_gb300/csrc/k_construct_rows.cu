@@ -24,7 +24,8 @@
 //    lane), zeroes the weights of visited cities (a byte per city in shared
 //    memory) and compacts the non-zero weights, in row order, into one of the
 //    ant's two buffers (a lane's offset is the count of the lanes before it,
-//    from three ballots of the count bits);
+//    from three ballots of the count bits).  Rows of up to 1024 entries keep
+//    no city ids there: the guess (below) keeps its index instead;
 //  * the chain warp: lane a adds ant a's compacted weights in order,
 //    s = fl(s + w) (sum_prob += prob_ptr[i], partial_sum += prob_ptr[i],
 //    src/Colony.cu:814,840), writes every running sum over its weight, and
@@ -37,20 +38,26 @@
 // compacts the row of its guessed pick into its other buffer, and from that
 // row's weights, still in registers, guesses the pick after it (an
 // approximate prefix: chunk sums, a scan over chunks and lanes, the same
-// crossing rule).  After its chain, lane a of the chain warp finds ant a's
-// exact pick: rnd = fl(u * S) (src/Colony.cu:826-828); the first 32-entry
-// block whose recorded end sum exceeds rnd, then in that block the first
-// running sum with !(sum <= rnd) -- written sum > rnd || rnd is NaN, as in
-// the k <= 32 step loop -- is the pick (sums never decrease, so both are
-// binary searches), and hands it back (named barrier C).  No crossing
-// (S <= 0, u * S rounding to S, or S = +inf from an infinite weight) takes
-// the fallback, as the reference does (chooseBestNext / select_local_best).
+// crossing rule); it then issues the loads of that guessed row into the
+// registers the scan just freed, so they are in flight while it waits for
+// the chain and passes the barriers.  After its chain, lane a of the chain
+// warp finds ant a's exact pick: rnd = fl(u * S) (src/Colony.cu:826-828);
+// the first 32-entry block whose recorded end sum exceeds rnd, then in that
+// block the first running sum with !(sum <= rnd) -- written sum > rnd || rnd
+// is NaN, as in the k <= 32 step loop -- is the pick (sums never decrease,
+// so both are binary searches), and hands it back with named barrier C, a
+// bar.red that also tells every scan warp whether every pick of the CTA was
+// its guess (the common case reads nothing back).  No crossing (S <= 0,
+// u * S rounding to S, or S = +inf from an infinite weight) takes the
+// fallback, as the reference does (chooseBestNext / select_local_best).
 // A right guess (nearly always: the approximate and the exact prefix differ
 // by a few ulps) leaves the next row compacted before the chain ends, so row
-// loads and scans stay off the critical path; a wrong one is undone and the
-// row of the real pick is scanned.  (The rows once went through shared memory
-// by TMA bulk copies, one row ahead; reading them from L2 in the scan, with
-// eight loads in flight a lane, measured faster and needs no mbarriers.)
+// loads and scans stay off the critical path; a wrong one is undone, the
+// pick's city found again from its index (rows without ids: the row's
+// unvisited entries counted again) and its row scanned.  (The rows once went
+// through shared memory by TMA bulk copies, one row ahead; reading them from
+// L2 in the scan, with eight loads in flight a lane, measured faster and
+// needs no mbarriers.)
 //
 // Every warp of a CTA passes the two named barriers once per step, n - 1
 // steps per item, with no early exit: an inconsistency is recorded in the
@@ -68,10 +75,11 @@ namespace aco {
 // S = rows_slots(K), P = ldk:
 //   w[2]:  2 x S f32        compacted weights (two buffers); the chain warp
 //                           overwrites each weight with the running sum
-//   id[2]: 2 x S int16      their city ids
+//   id[2]: 2 x S int16      their city ids (rows longer than 1024 entries)
 //   bend:  S/32 f32         running sum at the end of every 32 entries
-//   tw:    tabu bits        visited cities, 32 a word (words padded to 4; the
-//                           fallback's scans read them)
+//   tw:    tabu bits        visited cities, 32 a word (words padded to 4),
+//                           rebuilt from the bytes by the fallback, which
+//                           scans them
 //   tb:    tabu bytes       visited cities, 0xff or 0 (the scan's lookups: a
 //                           sign-extended byte is the AND mask itself)
 // Buffer b is addressed arithmetically (no array of pointers, which a
