@@ -753,6 +753,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
       RowsScan g;
       g.cnt = 0;
       g.guess = -1;
+      g.gidx = -1;
       int todo = -1;  // city whose row goes into buffer b ^ 1 in this pass
       bool ahead = false, hit = false;
       int next = cur;
