@@ -338,25 +338,21 @@ __device__ __forceinline__ int rows_guess_smem(const float *w, const int16_t *id
   return id[rows_swz(blk * 32 + __ffs(hit) - 1)];
 }
 
-// Chunks of 128 entries of the next step's row loaded ahead, across the
-// barriers (their registers stay live through the whole step).  All eight:
-// loading half of them ahead measured slower, and so did freeing the
-// registers for more ants a CTA (13 to 15 ants spill at their lower
-// register cap).
-constexpr int kRowsAhead = 8;
-
 struct RowsScan {
   int cnt;    // non-zero weights written
   int guess;  // approximate pick (u >= 0), or -1
   int gidx;   // its index in the compacted buffer (rows of one round)
 };
 
-// Loads chunks J0 .. J1 - 1 of round j0 of a city's row from L2 into
-// registers: lane l takes row positions j0 + 128j + 4l .. +3 of chunk j
-// (16-byte weight loads, 8-byte id loads, all before any use).  For an ant
-// that blends its fitness the weights are formed from tau and eta as they
-// arrive.
-template <int JB, int J0 = 0, int J1 = JB>
+// Loads round j0 of a city's row from L2 into registers: lane l takes row
+// positions j0 + 128j + 4l .. +3 of chunk j (16-byte weight loads, 8-byte id
+// loads, all JB chunks before any use).  For an ant that blends its fitness
+// the weights are formed from tau and eta as they arrive.  Round 0 of the
+// next step's row is loaded ahead this way, across the barriers (its
+// registers stay live through the whole step): loading only half of it
+// ahead measured slower, and so did freeing registers for more ants a CTA
+// (13 to 15 ants spill at their lower register cap).
+template <int JB>
 __device__ __forceinline__ void rows_load(const ColonyDev &c, int city, int j0, bool blend,
                                           float meanc, float ratio, int lane, uint4 (&q)[JB],
                                           uint2 (&ip)[JB]) {
@@ -365,7 +361,7 @@ __device__ __forceinline__ void rows_load(const ColonyDev &c, int city, int j0, 
   const float *grow = (blend ? c.tau_nn : c.choice_nn) + (size_t)city * c.ldk;
   const int16_t *irow = c.nn16 + (size_t)city * c.ldk;
 #pragma unroll
-  for (int j = J0; j < J1; j++) {
+  for (int j = 0; j < JB; j++) {
     const int p0 = j0 + j * 128 + lane * 4;
     const bool in = p0 < K;  // p0 < K <= ldk, ldk % 4 == 0: the four entries are in the row
     ip[j] = in ? __ldg(reinterpret_cast<const uint2 *>(irow + p0)) : make_uint2(0u, 0u);
@@ -404,9 +400,7 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
 #pragma unroll 1
   for (int j0 = 0; j0 < K; j0 += JB * 128) {
     unsigned nz = 0u;  // keep bits, four a chunk: chunk j at bits 4j .. 4j+3
-    if (loaded && j0 == 0)  // chunks 0 .. kRowsAhead - 1 are in q/ip already
-      rows_load<JB, kRowsAhead, JB>(c, city, j0, blend, meanc, ratio, lane, q, ip);
-    else
+    if (!(loaded && j0 == 0))  // round 0 may be in q/ip already
       rows_load<JB>(c, city, j0, blend, meanc, ratio, lane, q, ip);
 #pragma unroll
     for (int j = 0; j < JB; j++) {
@@ -730,7 +724,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
         gidx = r0.gidx;
       }
       if (guess >= 0 && !a.blend) {
-        rows_load<8, 0, kRowsAhead>(c, guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
+        rows_load<8>(c, guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
         pre = guess;
       }
     }
@@ -775,7 +769,7 @@ __device__ __forceinline__ void rows_item(const ColonyDev &c, int first, int cou
           todo = -1;
           pre = -1;
           if (g.guess >= 0 && !a.blend) {  // the next step's row, loaded across the barriers
-            rows_load<8, 0, kRowsAhead>(c, g.guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
+            rows_load<8>(c, g.guess, 0, false, 0.0f, 0.0f, lane, rq, rip);
             pre = g.guess;
           }
         }
