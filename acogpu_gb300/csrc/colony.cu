@@ -205,11 +205,6 @@ int create_common(const aco_params *params, int32_t n, aco_colony **out, aco_col
   }
   c->own_stream = true;
   for (int i = 0; i < 4; i++) cudaEventCreate(&c->ev[i]);
-  if (cudaMallocHost(&c->h_state, sizeof(ColonyState)) != cudaSuccess) {
-    c->h_state = nullptr;
-    aco_colony_destroy(c);
-    return ACO_ERR_OUT_OF_MEMORY;
-  }
   *cp = c;
   if ((s = allocate(c))) {
     aco_colony_destroy(c);
@@ -241,12 +236,17 @@ int device_error(aco_colony *c) {
 int read_state(aco_colony *c, ColonyState *h) {
   if (!c->initialized) return fail(c, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
   if (!c->state_fresh) {
+    if (!c->h_state && cudaMallocHost(&c->h_state, sizeof(ColonyState)) != cudaSuccess) {
+      c->h_state = nullptr;
+      return fail(c, ACO_ERR_OUT_OF_MEMORY, "cudaMallocHost");
+    }
     ACO_CUDA(c, cudaMemcpyAsync(c->h_state, c->st, sizeof(*h), cudaMemcpyDeviceToHost, c->stream),
              "read state");
     ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+    c->h_cache = *c->h_state;
     c->state_fresh = true;
   }
-  *h = *c->h_state;
+  *h = c->h_cache;
   return ACO_OK;
 }
 
@@ -480,7 +480,13 @@ namespace {
 // The device work of aco_colony_initialize, enqueued on the colony's stream
 // (the libm heuristic table, read back to the host, is the one wait); the
 // caller checks the device state before the colony counts as initialised.
-int initialize_enqueue(aco_colony *c) {
+// The setup of an initialised colony, in three parts so that a batch can
+// run every instance's first part before any host wait: init_begin resets
+// the state and starts the heuristic (the whole of it on the device; in the
+// libm mode the largest distance, into *dmax, which the host reads back),
+// init_heuristic_table finishes the libm mode from that distance, init_rest
+// does the rest (nn-lists, tau0, the ants).
+int init_begin(aco_colony *c, int32_t *dmax) {
   state_changed(c);
   drop_graph(c);
   c->initialized = false;
@@ -488,37 +494,40 @@ int initialize_enqueue(aco_colony *c) {
   // RankBasedAntSystem::computeParameters (src/RankBasedAntSystem.cu:31-36)
   if (c->p.variant == ACO_RANK_BASED && c->p.rank_w > n) c->p.rank_w = n;
   ACO_CUDA(c, cudaMemsetAsync(c->st, 0, sizeof(ColonyState), c->stream), "reset state");
-
   // heuristic (Colony::computeHurestics, src/Colony.cu:232-246)
   if (c->p.heuristic == ACO_HEURISTIC_DEVICE) {
     ACO_CUDA(c, launch_heuristic_device(c->dist, n, c->ld, c->p.beta, c->eta, c->stream),
              "heuristic");
   } else {
-    int32_t *dmax = nullptr;
-    ACO_CUDA(c, cudaMallocAsync(&dmax, 4, c->stream), "alloc");
     ACO_CUDA(c, cudaMemsetAsync(dmax, 0, 4, c->stream), "memset");
     ACO_CUDA(c, launch_max_distance(c->dist, n, c->ld, dmax, c->stream), "max distance");
-    int32_t hmax = 0;
-    ACO_CUDA(c, cudaMemcpyAsync(&hmax, dmax, 4, cudaMemcpyDeviceToHost, c->stream), "read max");
-    ACO_CUDA(c, cudaFreeAsync(dmax, c->stream), "free");
-    ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
-    if (hmax < 0 || hmax >= (1 << 26))
-      return fail(c, ACO_ERR_UNSUPPORTED, "distances too large for the libm heuristic table");
-    // HURESTIC(d, beta) of the reference CPU build (inc/Colony.h:20), one
-    // entry per distinct distance value.
-    std::vector<float> table((size_t)hmax + 1);
-    for (int32_t d = 0; d <= hmax; d++) table[d] = powf((float)(1.0 / ((float)d)), c->p.beta);
-    float *dtab = nullptr;
-    ACO_CUDA(c, cudaMallocAsync(&dtab, table.size() * 4, c->stream), "alloc table");
-    ACO_CUDA(c, cudaMemcpyAsync(dtab, table.data(), table.size() * 4, cudaMemcpyHostToDevice,
-                                c->stream),
-             "upload table");
-    ACO_CUDA(c, launch_heuristic_table(c->dist, n, c->ld, dtab, hmax + 1, c->eta, c->st, c->stream),
-             "heuristic table");
-    ACO_CUDA(c, cudaFreeAsync(dtab, c->stream), "free table");
-    ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
   }
+  return ACO_OK;
+}
 
+// The libm mode's table, HURESTIC(d, beta) of the reference CPU build
+// (inc/Colony.h:20), one entry per distinct distance value, built on the
+// host into `table` (which the caller keeps until the stream has run) and
+// applied by a kernel.
+int init_heuristic_table(aco_colony *c, int32_t hmax, std::vector<float> &table) {
+  if (hmax < 0 || hmax >= (1 << 26))
+    return fail(c, ACO_ERR_UNSUPPORTED, "distances too large for the libm heuristic table");
+  table.resize((size_t)hmax + 1);
+  for (int32_t d = 0; d <= hmax; d++) table[d] = powf((float)(1.0 / ((float)d)), c->p.beta);
+  float *dtab = nullptr;
+  ACO_CUDA(c, cudaMallocAsync(&dtab, table.size() * 4, c->stream), "alloc table");
+  ACO_CUDA(c, cudaMemcpyAsync(dtab, table.data(), table.size() * 4, cudaMemcpyHostToDevice,
+                              c->stream),
+           "upload table");
+  ACO_CUDA(c, launch_heuristic_table(c->dist, c->n, c->ld, dtab, hmax + 1, c->eta, c->st,
+                                     c->stream),
+           "heuristic table");
+  ACO_CUDA(c, cudaFreeAsync(dtab, c->stream), "free table");
+  return ACO_OK;
+}
+
+int init_rest(aco_colony *c) {
+  const int n = c->n;
   // nn-list (Colony::computeNNlist, src/Colony.cu:276-311)
   if (c->p.nn_order == ACO_NN_STABLE) {
     ACO_CUDA(c, launch_nn_sort_stable(c->dist, n, c->ld, c->K, c->ldk, c->nn, c->st, c->stream,
@@ -574,6 +583,24 @@ int initialize_enqueue(aco_colony *c) {
   if (int s0 = plan_construction(c)) return s0;
   ACO_CUDA(c, launch_pheromone_rows(d, false, false, false, c->stream), "choice rows");
   return ACO_OK;
+}
+
+// One colony's whole setup, with the libm mode's one read-back in the middle.
+int initialize_enqueue(aco_colony *c) {
+  const bool libm = c->p.heuristic != ACO_HEURISTIC_DEVICE;
+  int32_t *dmax = nullptr;
+  if (libm) ACO_CUDA(c, cudaMallocAsync(&dmax, 4, c->stream), "alloc");
+  if (int s = init_begin(c, dmax)) return s;
+  if (libm) {
+    int32_t hmax = 0;
+    ACO_CUDA(c, cudaMemcpyAsync(&hmax, dmax, 4, cudaMemcpyDeviceToHost, c->stream), "read max");
+    ACO_CUDA(c, cudaFreeAsync(dmax, c->stream), "free");
+    ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+    std::vector<float> table;
+    if (int s = init_heuristic_table(c, hmax, table)) return s;
+    ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
+  }
+  return init_rest(c);
 }
 
 }  // namespace
@@ -946,6 +973,7 @@ struct aco_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int64_t launches = 0;
+  ColonyState *h_states = nullptr;  // pinned, one a instance (the first batch read allocates it)
   std::string err;
 };
 
@@ -1109,11 +1137,43 @@ int batch_enqueue(aco_batch *b, bool construct, bool epilogue, bool rows, bool u
   return ACO_OK;
 }
 
-int batch_state_check(aco_batch *b) {
+// The state words of every instance whose copy on the host is stale: their
+// read-backs queued on the batch stream (the instances' own stream between
+// calls), then one wait -- rather than a wait per instance.  The getters
+// want initialised instances; the error check does not.
+int batch_read_states(aco_batch *b, bool need_init) {
+  if (!b->h_states &&
+      cudaMallocHost(&b->h_states, b->cols.size() * sizeof(ColonyState)) != cudaSuccess) {
+    b->h_states = nullptr;
+    return bfail(b, ACO_ERR_OUT_OF_MEMORY, "cudaMallocHost");
+  }
+  for (size_t i = 0; i < b->cols.size(); i++) {
+    aco_colony *c = b->cols[i];
+    if (need_init && !c->initialized)
+      return bfail(b, ACO_ERR_NOT_INITIALIZED, "colony not initialized");
+    if (c->state_fresh) continue;
+    ACO_BCUDA(b, cudaMemcpyAsync(&b->h_states[i], c->st, sizeof(ColonyState),
+                                 cudaMemcpyDeviceToHost, b->stream),
+              "read state");
+  }
   ACO_BCUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
-  for (aco_colony *c : b->cols) {
-    int s = device_error(c);
-    if (s) return bfail(b, s, c->err);
+  for (size_t i = 0; i < b->cols.size(); i++) {
+    aco_colony *c = b->cols[i];
+    if (c->state_fresh) continue;
+    c->h_cache = b->h_states[i];
+    c->state_fresh = c->initialized;  // the getters' copy, once there is one to keep
+  }
+  return ACO_OK;
+}
+
+// The device error words of every instance, after the batch stream has run.
+int batch_state_check(aco_batch *b) {
+  if (int s = batch_read_states(b, false)) return s;
+  for (size_t i = 0; i < b->cols.size(); i++) {
+    aco_colony *c = b->cols[i];
+    const uint32_t err = c->state_fresh ? c->h_cache.error : b->h_states[i].error;
+    if (err & kErrTimeout) return bfail(b, ACO_ERR_DEVICE_TIMEOUT, "a bounded device wait expired");
+    if (err & kErrCheck) return bfail(b, ACO_ERR_DEVICE_CHECK, "a device-side check failed");
   }
   return ACO_OK;
 }
@@ -1202,14 +1262,40 @@ int aco_batch_initialize(aco_batch *b) {
     if (cudaStreamCreateWithFlags(&pool[q], cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamWaitEvent(pool[q], ready, 0) != cudaSuccess)
       s = bfail(b, ACO_ERR_CUDA, "initialize: streams");
-  for (size_t i = 0; i < b->cols.size() && !s; i++) {
+  // In the libm heuristic mode every instance's largest distance is read
+  // back once, for all of them after their first part, rather than with a
+  // wait per instance (the host tables live until the final wait).
+  const size_t ni = b->cols.size();
+  const bool libm = b->p.heuristic != ACO_HEURISTIC_DEVICE;
+  int32_t *d_hmax = nullptr;
+  std::vector<int32_t> hmax(ni, 0);
+  std::vector<std::vector<float>> tables(ni);
+  if (!s && libm && cudaMalloc(&d_hmax, ni * sizeof(int32_t)) != cudaSuccess)
+    s = bfail(b, ACO_ERR_OUT_OF_MEMORY, "initialize: alloc");
+  for (size_t i = 0; i < ni && !s; i++) {
     aco_colony *c = b->cols[i];
     c->stream = pool[i % npool];
-    if (int e = initialize_enqueue(c)) s = bfail(b, e, c->err);
+    if (int e = init_begin(c, libm ? d_hmax + i : nullptr)) s = bfail(b, e, c->err);
+  }
+  if (libm) {
+    for (int q = 0; q < npool; q++)
+      if (pool[q] && cudaStreamSynchronize(pool[q]) != cudaSuccess && !s)
+        s = bfail(b, ACO_ERR_CUDA, "initialize: synchronize");
+    if (!s && cudaMemcpy(hmax.data(), d_hmax, ni * sizeof(int32_t), cudaMemcpyDeviceToHost) !=
+                  cudaSuccess)
+      s = bfail(b, ACO_ERR_CUDA, "initialize: read max");
+  }
+  for (size_t i = 0; i < ni && !s; i++) {
+    aco_colony *c = b->cols[i];
+    if (libm)
+      if (int e = init_heuristic_table(c, hmax[i], tables[i])) s = bfail(b, e, c->err);
+    if (!s)
+      if (int e = init_rest(c)) s = bfail(b, e, c->err);
   }
   for (int q = 0; q < npool; q++)
     if (pool[q] && cudaStreamSynchronize(pool[q]) != cudaSuccess && !s)
       s = bfail(b, ACO_ERR_CUDA, "initialize: synchronize");
+  if (d_hmax) cudaFree(d_hmax);
   for (aco_colony *c : b->cols) c->stream = b->stream;
   for (int q = 0; q < npool; q++)
     if (pool[q]) cudaStreamDestroy(pool[q]);
@@ -1472,7 +1558,7 @@ int aco_batch_get_colony(aco_batch *b, int32_t i, aco_colony **out) {
 
 int aco_batch_get_glob_best(aco_batch *b, int64_t *out) {
   if (!b || !out) return ACO_ERR_INVALID_ARGUMENT;
-  ACO_BCUDA(b, cudaStreamSynchronize(b->stream), "synchronize");
+  if (int s = batch_read_states(b, true)) return s;
   for (size_t i = 0; i < b->cols.size(); i++) {
     int s = aco_colony_get_glob_best(b->cols[i], &out[i]);
     if (s) return bfail(b, s, b->cols[i]->err);
@@ -1482,6 +1568,7 @@ int aco_batch_get_glob_best(aco_batch *b, int64_t *out) {
 
 int aco_batch_get_tours_built(aco_batch *b, int64_t *out) {
   if (!b || !out) return ACO_ERR_INVALID_ARGUMENT;
+  if (int s = batch_read_states(b, true)) return s;
   int64_t total = 0;
   for (aco_colony *c : b->cols) {
     aco_stats st;
@@ -1510,6 +1597,7 @@ void aco_batch_destroy(aco_batch *b) {
   if (b->d_rowmap) cudaFree(b->d_rowmap);
   if (b->d_items) cudaFree(b->d_items);
   if (b->d_queue) cudaFree(b->d_queue);
+  if (b->h_states) cudaFreeHost(b->h_states);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }

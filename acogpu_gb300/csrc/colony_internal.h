@@ -52,9 +52,12 @@ struct aco_colony {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  // Host copy of the device state block (pinned), valid until the next call
-  // that enqueues work on the colony: the getters of one iteration share one
-  // device-to-host read.
+  // Host copy of the device state block, valid until the next call that
+  // enqueues work on the colony: the getters of one iteration share one
+  // device-to-host read.  A colony read on its own stages it through a
+  // pinned word allocated at its first read; a batch reads all its
+  // instances through one pinned array of its own.
+  aco::ColonyState h_cache{};
   aco::ColonyState *h_state = nullptr;
   bool state_fresh = false;
   std::string err;
