@@ -58,12 +58,18 @@ int cuda_fail(aco_colony *c, cudaError_t e, const char *what) {
 // of a colony reports out-of-memory without allocating (-1: off).
 std::atomic<int> g_fail_alloc{-1};
 
-template <class T>
-int dalloc(aco_colony *c, T **ptr, size_t count) {
+// Counts one allocation against the injected failure; true if it fails.
+bool injected_failure() {
   int k = g_fail_alloc.load();
   while (k >= 0 && !g_fail_alloc.compare_exchange_weak(k, k - 1)) {
   }
-  if (k == 0) return fail(c, ACO_ERR_OUT_OF_MEMORY, "cudaMalloc: injected allocation failure");
+  return k == 0;
+}
+
+template <class T>
+int dalloc(aco_colony *c, T **ptr, size_t count) {
+  if (injected_failure())
+    return fail(c, ACO_ERR_OUT_OF_MEMORY, "cudaMalloc: injected allocation failure");
   void *p = nullptr;
   cudaError_t e = cudaMalloc(&p, count * sizeof(T) + 16);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
@@ -71,6 +77,37 @@ int dalloc(aco_colony *c, T **ptr, size_t count) {
   *ptr = static_cast<T *>(p);
   return ACO_OK;
 }
+
+// A colony's arrays from one device allocation (a cudaMalloc costs tens of
+// microseconds, and a batch creates a few hundred arrays): the requests are
+// listed first, then each counts against the injected failure in turn, then
+// one block is allocated and carved at 256-byte boundaries (16 bytes of
+// slack past each array, as dalloc leaves).
+struct Carve {
+  std::vector<std::pair<void **, size_t>> req;
+  template <class T>
+  void add(T **ptr, size_t count) {
+    req.emplace_back(reinterpret_cast<void **>(ptr), count * sizeof(T) + 16);
+  }
+  int commit(aco_colony *c) {
+    size_t total = 0;
+    for (const auto &r : req) {
+      if (injected_failure())
+        return fail(c, ACO_ERR_OUT_OF_MEMORY, "cudaMalloc: injected allocation failure");
+      total += (r.second + 255) / 256 * 256;
+    }
+    void *base = nullptr;
+    const cudaError_t e = cudaMalloc(&base, total);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+    c->allocations.push_back(base);
+    char *p = static_cast<char *>(base);
+    for (const auto &r : req) {
+      *r.first = p;
+      p += (r.second + 255) / 256 * 256;
+    }
+    return ACO_OK;
+  }
+};
 
 ColonyDev make_dev(const aco_colony *c) {
   ColonyDev d;
@@ -136,29 +173,28 @@ int check_params(const aco_params *p, int n) {
 int allocate(aco_colony *c) {
   const size_t n = c->n, m = c->m, ld = c->ld, ldk = c->ldk, ldm = c->ldm;
   int s;
-  if ((s = dalloc(c, &c->dist, n * ld))) return s;
-  if ((s = dalloc(c, &c->eta, n * ld))) return s;
-  if ((s = dalloc(c, &c->tau, n * ld))) return s;
-  if ((s = dalloc(c, &c->choice, n * ld))) return s;
-  if ((s = dalloc(c, &c->nn, n * ldk))) return s;
-  if ((s = dalloc(c, &c->eta_nn, n * ldk))) return s;
-  if ((s = dalloc(c, &c->choice_nn, n * ldk))) return s;
-  if ((s = dalloc(c, &c->tau_nn, c->p.aging ? n * ldk : 32))) return s;
-  if ((s = dalloc(c, &c->tours, m * ld))) return s;
-  if ((s = dalloc(c, &c->newlen, m))) return s;
-  if ((s = dalloc(c, &c->len, m))) return s;
-  if ((s = dalloc(c, &c->succT, n * ldm))) return s;
-  if ((s = dalloc(c, &c->predT, n * ldm))) return s;
-  if ((s = dalloc(c, &c->gbtour, n))) return s;
-  if ((s = dalloc(c, &c->age, m))) return s;
-  if ((s = dalloc(c, &c->perf, m))) return s;
-  if ((s = dalloc(c, &c->valid, m))) return s;
-  if ((s = dalloc(c, &c->mean, ld))) return s;
+  Carve a;
+  a.add(&c->dist, n * ld);
+  a.add(&c->eta, n * ld);
+  a.add(&c->tau, n * ld);
+  a.add(&c->choice, n * ld);
+  a.add(&c->nn, n * ldk);
+  a.add(&c->eta_nn, n * ldk);
+  a.add(&c->choice_nn, n * ldk);
+  a.add(&c->tau_nn, c->p.aging ? n * ldk : 32);
+  a.add(&c->tours, m * ld);
+  a.add(&c->newlen, m);
+  a.add(&c->len, m);
+  a.add(&c->succT, n * ldm);
+  a.add(&c->predT, n * ldm);
+  a.add(&c->gbtour, n);
+  a.add(&c->age, m);
+  a.add(&c->perf, m);
+  a.add(&c->valid, m);
+  a.add(&c->mean, ld);
   // Candidate ids as int16, for the k <= 32 kernels and the long-row kernel
   // (16 bytes of slack: the cluster kernel stages slices in 16-byte units).
-  if ((c->K <= 32 ? c->n < 32768 : c->n <= kRowsMaxCities) &&
-      (s = dalloc(c, &c->nn16, n * ldk + 8)))
-    return s;
+  if (c->K <= 32 ? c->n < 32768 : c->n <= kRowsMaxCities) a.add(&c->nn16, n * ldk + 8);
   // The fallback's second tier, for the k <= 32 step loop.
   const bool tier = c->p.fallback_tier == ACO_FALLBACK_TIER_ON ||
                     (c->p.fallback_tier == ACO_FALLBACK_TIER_AUTO &&
@@ -166,14 +202,15 @@ int allocate(aco_colony *c) {
   c->t2 = (tier && c->K <= 32 && c->n < 32768) ? std::min(kTier2, c->n - 1 - c->K) : 0;
   if (c->t2 < 0) c->t2 = 0;
   if (c->t2 > 0) {
-    if ((s = dalloc(c, &c->nn2, n * kTier2))) return s;
-    if ((s = dalloc(c, &c->t2v, n * kTier2))) return s;
-    if ((s = dalloc(c, &c->mout, n))) return s;
+    a.add(&c->nn2, n * kTier2);
+    a.add(&c->t2v, n * kTier2);
+    a.add(&c->mout, n);
   }
-  if ((s = dalloc(c, &c->plan, m + 2))) return s;
-  if ((s = dalloc(c, &c->dep_col, m + 1))) return s;
-  if ((s = dalloc(c, &c->dep_delta, m + 1))) return s;
-  if ((s = dalloc(c, &c->st, 1))) return s;
+  a.add(&c->plan, m + 2);
+  a.add(&c->dep_col, m + 1);
+  a.add(&c->dep_delta, m + 1);
+  a.add(&c->st, 1);
+  if ((s = a.commit(c))) return s;
   ACO_CUDA(c, cudaMemsetAsync(c->tours, 0, m * ld * 4, c->stream), "memset tours");
   ACO_CUDA(c, cudaMemsetAsync(c->st, 0, sizeof(ColonyState), c->stream), "memset state");
   ACO_CUDA(c, cudaMemsetAsync(c->gbtour, 0, n * 4, c->stream), "memset gbtour");
