@@ -543,23 +543,23 @@ int init_begin(aco_colony *c, int32_t *dmax) {
 }
 
 // The libm mode's table, HURESTIC(d, beta) of the reference CPU build
-// (inc/Colony.h:20), one entry per distinct distance value, built on the
-// host into `table` (which the caller keeps until the stream has run) and
-// applied by a kernel.
-int init_heuristic_table(aco_colony *c, int32_t hmax, std::vector<float> &table) {
-  if (hmax < 0 || hmax >= (1 << 26))
-    return fail(c, ACO_ERR_UNSUPPORTED, "distances too large for the libm heuristic table");
+// (inc/Colony.h:20), one entry per distinct distance value d = 0 .. hmax,
+// on the host.  It depends on beta and hmax alone, so a batch builds one up
+// to its largest distance and every instance reads its own prefix.
+bool libm_table(int32_t hmax, float beta, std::vector<float> &table) {
+  if (hmax < 0 || hmax >= (1 << 26)) return false;
   table.resize((size_t)hmax + 1);
-  for (int32_t d = 0; d <= hmax; d++) table[d] = powf((float)(1.0 / ((float)d)), c->p.beta);
-  float *dtab = nullptr;
-  ACO_CUDA(c, cudaMallocAsync(&dtab, table.size() * 4, c->stream), "alloc table");
-  ACO_CUDA(c, cudaMemcpyAsync(dtab, table.data(), table.size() * 4, cudaMemcpyHostToDevice,
-                              c->stream),
-           "upload table");
-  ACO_CUDA(c, launch_heuristic_table(c->dist, c->n, c->ld, dtab, hmax + 1, c->eta, c->st,
+  for (int32_t d = 0; d <= hmax; d++) table[d] = powf((float)(1.0 / ((float)d)), beta);
+  return true;
+}
+const char *const kTooFar = "distances too large for the libm heuristic table";
+
+// eta from a table already on the device (entries > the colony's largest
+// distance).
+int init_heuristic_table(aco_colony *c, const float *dtab, int32_t entries) {
+  ACO_CUDA(c, launch_heuristic_table(c->dist, c->n, c->ld, dtab, entries, c->eta, c->st,
                                      c->stream),
            "heuristic table");
-  ACO_CUDA(c, cudaFreeAsync(dtab, c->stream), "free table");
   return ACO_OK;
 }
 
@@ -634,7 +634,14 @@ int initialize_enqueue(aco_colony *c) {
     ACO_CUDA(c, cudaFreeAsync(dmax, c->stream), "free");
     ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
     std::vector<float> table;
-    if (int s = init_heuristic_table(c, hmax, table)) return s;
+    if (!libm_table(hmax, c->p.beta, table)) return fail(c, ACO_ERR_UNSUPPORTED, kTooFar);
+    float *dtab = nullptr;
+    ACO_CUDA(c, cudaMallocAsync(&dtab, table.size() * 4, c->stream), "alloc table");
+    ACO_CUDA(c, cudaMemcpyAsync(dtab, table.data(), table.size() * 4, cudaMemcpyHostToDevice,
+                                c->stream),
+             "upload table");
+    if (int s = init_heuristic_table(c, dtab, hmax + 1)) return s;
+    ACO_CUDA(c, cudaFreeAsync(dtab, c->stream), "free table");
     ACO_CUDA(c, cudaStreamSynchronize(c->stream), "synchronize");
   }
   return init_rest(c);
@@ -1301,12 +1308,13 @@ int aco_batch_initialize(aco_batch *b) {
       s = bfail(b, ACO_ERR_CUDA, "initialize: streams");
   // In the libm heuristic mode every instance's largest distance is read
   // back once, for all of them after their first part, rather than with a
-  // wait per instance (the host tables live until the final wait).
+  // wait per instance; one table up to the largest serves every instance.
   const size_t ni = b->cols.size();
   const bool libm = b->p.heuristic != ACO_HEURISTIC_DEVICE;
   int32_t *d_hmax = nullptr;
+  float *d_table = nullptr;
+  int32_t entries = 0;
   std::vector<int32_t> hmax(ni, 0);
-  std::vector<std::vector<float>> tables(ni);
   if (!s && libm && cudaMalloc(&d_hmax, ni * sizeof(int32_t)) != cudaSuccess)
     s = bfail(b, ACO_ERR_OUT_OF_MEMORY, "initialize: alloc");
   for (size_t i = 0; i < ni && !s; i++) {
@@ -1321,11 +1329,19 @@ int aco_batch_initialize(aco_batch *b) {
     if (!s && cudaMemcpy(hmax.data(), d_hmax, ni * sizeof(int32_t), cudaMemcpyDeviceToHost) !=
                   cudaSuccess)
       s = bfail(b, ACO_ERR_CUDA, "initialize: read max");
+    std::vector<float> table;
+    const int32_t hm = s ? 0 : *std::max_element(hmax.begin(), hmax.end());
+    if (!s && !libm_table(hm, b->p.beta, table)) s = bfail(b, ACO_ERR_UNSUPPORTED, kTooFar);
+    entries = (int32_t)table.size();
+    if (!s && (cudaMalloc(&d_table, table.size() * 4) != cudaSuccess ||
+               cudaMemcpy(d_table, table.data(), table.size() * 4, cudaMemcpyHostToDevice) !=
+                   cudaSuccess))
+      s = bfail(b, ACO_ERR_CUDA, "initialize: upload table");
   }
   for (size_t i = 0; i < ni && !s; i++) {
     aco_colony *c = b->cols[i];
     if (libm)
-      if (int e = init_heuristic_table(c, hmax[i], tables[i])) s = bfail(b, e, c->err);
+      if (int e = init_heuristic_table(c, d_table, entries)) s = bfail(b, e, c->err);
     if (!s)
       if (int e = init_rest(c)) s = bfail(b, e, c->err);
   }
@@ -1333,6 +1349,7 @@ int aco_batch_initialize(aco_batch *b) {
     if (pool[q] && cudaStreamSynchronize(pool[q]) != cudaSuccess && !s)
       s = bfail(b, ACO_ERR_CUDA, "initialize: synchronize");
   if (d_hmax) cudaFree(d_hmax);
+  if (d_table) cudaFree(d_table);
   for (aco_colony *c : b->cols) c->stream = b->stream;
   for (int q = 0; q < npool; q++)
     if (pool[q]) cudaStreamDestroy(pool[q]);
