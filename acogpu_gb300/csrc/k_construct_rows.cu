@@ -456,13 +456,15 @@ __device__ __forceinline__ RowsScan rows_scan(const ColonyDev &c, const RowsAnt 
 }
 
 // Exact pick (see the header) of one ant by one lane: rnd = fl(u * S), the
-// first block of 32 whose recorded end sum passes rnd, then in the running
-// sums pf that the chain wrote over that block the first entry with
-// !(pf <= rnd).  Entries past cnt hold S (the padding adds zeros) and are not
-// candidates.  The sums never decrease, so both searches are binary (a fixed
-// number of steps, the same in every lane); a NaN rnd (u = 0 with S = +inf,
-// or a NaN sum) passes at the first entry.  Index, or -1.
-__device__ __forceinline__ int rows_exact_lane(const float *pf, const float *bend, int cnt, int L,
+// first block of 32 whose recorded end sum passes rnd (the sums never
+// decrease, so a binary search, a fixed number of steps in every lane), then
+// in that block the first entry whose running sum has !(sum <= rnd): the
+// block's running sums formed again from the sum at the end of the block
+// before, by the chain's own adds in the chain's own order, so the same bits.
+// Entries past cnt (the padding adds zeros) are not candidates; a NaN rnd
+// (u = 0 with S = +inf, or a NaN sum) passes at the first entry.  Index, or
+// -1.
+__device__ __forceinline__ int rows_exact_lane(const float *w, const float *bend, int cnt, int L,
                                                float S, float u) {
   if (S <= 0.0f) return -1;  // chooseBestNext (src/Colony.cu:776-778)
   const float rnd = __fmul_rn(u, S);
@@ -474,11 +476,19 @@ __device__ __forceinline__ int rows_exact_lane(const float *pf, const float *ben
   for (; step > 0; step >>= 1)
     if (blk + step <= nb && bend[blk + step - 1] <= rnd) blk += step;
   if (blk >= nb) return -1;
-  // The block's last running sum is bend[blk] > rnd: at most 31 entries pass.
-  int e = 0;
-#pragma unroll
-  for (int t = 16; t > 0; t >>= 1)
-    if (pf[rows_swz(blk * 32 + e + t - 1)] <= rnd) e += t;
+  // The block's last running sum is bend[blk] > rnd, so one entry passes.
+  const float *wb = w + blk * 32;
+  const int key = blk & 3;
+  float s = blk > 0 ? bend[blk - 1] : 0.0f;
+  int e = 31;
+#pragma unroll 1
+  for (int t = 0; t < 32; t++) {
+    s = __fadd_rn(s, wb[t ^ key]);
+    if (s > rnd) {
+      e = t;
+      break;
+    }
+  }
   const int i = blk * 32 + e;
   return i < cnt ? i : -1;
 }
@@ -573,27 +583,23 @@ __device__ __forceinline__ bool named_bar_red_and(int id, int threads, bool pred
 // ---- chain warp --------------------------------------------------------------
 
 // Adds one block of 32 entries (slot g, logical component t at physical
-// component t ^ KEY) and writes each running sum where its weight was.
+// component t ^ KEY), in order.
 template <int KEY>
-__device__ __forceinline__ void rows_chain_add32(float4 *w4, const float4 (&a)[8], float &s) {
+__device__ __forceinline__ void rows_chain_add32(const float4 (&a)[8], float &s) {
 #pragma unroll
   for (int g = 0; g < 8; g++) {
     const float in[4] = {a[g].x, a[g].y, a[g].z, a[g].w};
-    float out[4];
 #pragma unroll
-    for (int t = 0; t < 4; t++) {
-      s = __fadd_rn(s, in[t ^ KEY]);
-      out[t ^ KEY] = s;
-    }
-    w4[g] = make_float4(out[0], out[1], out[2], out[3]);
+    for (int t = 0; t < 4; t++) s = __fadd_rn(s, in[t ^ KEY]);
   }
 }
 
-// Lane a < A: the running sums of ant a's buffer w over L entries (a multiple
-// of 32, zero-padded past its count), each written over its weight, the sum
-// at the end of every 32 entries in bend, the total in *S.  Four blocks of
-// 32 per trip (their swizzle keys 0..3), each block's weights read while the
-// previous block is added.
+// Lane a < A: the sequential sum of ant a's buffer w over L entries (a
+// multiple of 32, zero-padded past its count), with the running sum at the
+// end of every 32 entries in bend; returns the total S.  The running sums
+// inside the blocks are not kept: the exact pick forms those of its one
+// block again.  Four blocks of 32 per trip (their swizzle keys 0..3), each
+// block's weights read while the previous block is added.
 __device__ __forceinline__ float rows_chain(float *w, float *bend, int L) {
   float4 *w4 = reinterpret_cast<float4 *>(w);
   const int nb = L >> 5;
@@ -609,7 +615,7 @@ __device__ __forceinline__ float rows_chain(float *w, float *bend, int L) {
     if (bb >= nb) break;                                                   \
     const int nx = bb + 1 < nb ? bb + 1 : bb;                              \
     _Pragma("unroll") for (int g = 0; g < 8; g++) NXT[g] = w4[nx * 8 + g]; \
-    rows_chain_add32<KEY>(w4 + bb * 8, CUR, s);                            \
+    rows_chain_add32<KEY>(CUR, s);                                         \
     bend[bb] = s;                                                          \
   }
 #pragma unroll 1
