@@ -28,9 +28,9 @@
 //    no city ids there: the guess (below) keeps its index instead;
 //  * the chain warp: lane a adds ant a's compacted weights in order,
 //    s = fl(s + w) (sum_prob += prob_ptr[i], partial_sum += prob_ptr[i],
-//    src/Colony.cu:814,840), writes every running sum over its weight, and
-//    records the sum at the end of every 32 entries and the total S; then
-//    it finds ant a's exact pick (below).  The A chains and picks share one
+//    src/Colony.cu:814,840), records the sum at the end of every 32 entries
+//    and the total S, then finds ant a's exact pick (below), forming the
+//    running sums of the one block it needs again from that block's start.  The A chains and picks share one
 //    instruction stream.
 //
 // One step: the scan warps hand their buffers, with the step's uniform u,
@@ -73,8 +73,7 @@ namespace aco {
 // consecutive ants start four banks apart and the chain warp's 16-byte reads
 // of A buffers at once spread over the banks; offsets in rows_layout).
 // S = rows_slots(K), P = ldk:
-//   w[2]:  2 x S f32        compacted weights (two buffers); the chain warp
-//                           overwrites each weight with the running sum
+//   w[2]:  2 x S f32        compacted weights (two buffers)
 //   id[2]: 2 x S int16      their city ids (rows longer than 1024 entries)
 //   bend:  S/32 f32         running sum at the end of every 32 entries
 //   tw:    tabu bits        visited cities, 32 a word (words padded to 4),
