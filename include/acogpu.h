@@ -523,8 +523,9 @@ ACO_API void aco_tsplib_destroy(aco_tsplib *t);
  * finished and the flag has been read back; ACO_ERR_CUDA if the launch or
  * the copy failed.  The CUDA context stays usable.
  *
- * aco_debug_fail_allocation: the after-th next device allocation made by a
- * colony (0 = the next one) reports ACO_ERR_OUT_OF_MEMORY without
+ * aco_debug_fail_allocation: the after-th next device array requested by a
+ * colony (0 = the next one; a colony's arrays share one allocation, made
+ * once every request has passed) reports ACO_ERR_OUT_OF_MEMORY without
  * allocating; a negative value switches the injection off.  Process-wide. */
 ACO_API int aco_selftest_bounded_wait(uint32_t polls);
 ACO_API void aco_debug_fail_allocation(int32_t after);
